@@ -1,0 +1,414 @@
+// capi.cpp -- the extern "C" entry points of include/gpuh2h.h and
+// include/gpuh2h_tools.h.  Every call converts internal exceptions into a
+// status code and a per-thread message; nothing exits the process.
+#include <algorithm>
+#include <cstring>
+#include <mutex>
+#include <string>
+
+#include "graph.h"
+#include "gpuh2h_tools.h"
+
+namespace gh {
+void write_partition_rate(const Graph &g, const std::string &dir);
+void write_contract_csv(const Graph &g, const std::string &root);
+void write_construct_info(const Graph &g, const std::string &root);
+void write_query_result(const Graph &g, const std::string &root, int64_t qn, const int64_t *t19);
+const char *partition_file_prefix(int method);
+void generate_road(const h2h_gen_params &p, const std::string &root, const std::string &name, int64_t *n_arcs);
+void gen_uniform_pairs(int nv, int64_t n, uint64_t seed, int *x, int *y);
+void gen_local_pairs(const Graph &g, int64_t n, int hops, uint64_t seed, int *x, int *y);
+
+static thread_local std::string g_last_error;
+void set_last_error(const std::string &msg) { g_last_error = msg; }
+
+// Host-buffer query staging owned by a handle.
+struct HostQueryStage {
+  std::mutex mu;
+  int *dx = nullptr, *dy = nullptr, *dout = nullptr;
+  int64_t cap = 0;
+  cudaStream_t stream = nullptr;
+  ~HostQueryStage() {
+    cudaFree(dx); cudaFree(dy); cudaFree(dout);
+    if (stream) cudaStreamDestroy(stream);
+  }
+};
+
+}  // namespace gh
+
+struct h2h_graph {
+  gh::Graph g;
+  gh::HostQueryStage stage;
+};
+
+namespace {
+
+template <typename F>
+int guarded(F &&f) {
+  try {
+    f();
+    return H2H_OK;
+  } catch (const gh::Error &e) {
+    gh::set_last_error(e.what());
+    return e.code;
+  } catch (const std::bad_alloc &) {
+    gh::set_last_error("host allocation failed");
+    return H2H_ERR_NOMEM;
+  } catch (const std::exception &e) {
+    gh::set_last_error(e.what());
+    return H2H_ERR_STATE;
+  }
+}
+
+// Every arc u->v needs a reverse arc v->u: the partition-level kernel applies
+// the reference's pairwise fill-in per neighbour, which is the same only when
+// "u lists v" is symmetric (true for the both-directions Edge format).
+void check_symmetric(const gh::Graph &g) {
+  std::vector<uint64_t> a, b;
+  a.reserve(g.m);
+  for (int v = 0; v < g.n; v++)
+    for (int e = g.adj_off[v]; e < g.adj_off[v + 1]; e++) a.push_back(((uint64_t)v << 32) | (uint32_t)g.adj_v[e]);
+  std::sort(a.begin(), a.end());
+  a.erase(std::unique(a.begin(), a.end()), a.end());
+  b.resize(a.size());
+  for (size_t i = 0; i < a.size(); i++) b[i] = (a[i] << 32) | (a[i] >> 32);
+  std::sort(b.begin(), b.end());
+  GH_CHECK(a == b, H2H_ERR_UNSUPPORTED, "Edge file lists an arc without its reverse arc");
+}
+
+void check_connected(const gh::Graph &g) {
+  std::vector<char> seen(g.n, 0);
+  std::vector<int> st{0};
+  seen[0] = 1;
+  int cnt = 1;
+  while (!st.empty()) {
+    int v = st.back();
+    st.pop_back();
+    for (int e = g.adj_off[v]; e < g.adj_off[v + 1]; e++) {
+      int u = g.adj_v[e];
+      if (!seen[u]) { seen[u] = 1; cnt++; st.push_back(u); }
+    }
+  }
+  GH_CHECK(cnt == g.n, H2H_ERR_UNSUPPORTED,
+           "graph is disconnected (the reference's elimination reads out of bounds on such input)");
+}
+
+int load_common(const std::string &edge, const std::string &idf, const std::string &cut, const char *name, int H,
+                int C, int threads, int method, h2h_graph **out) {
+  if (!out) { gh::set_last_error("out is NULL"); return H2H_ERR_ARG; }
+  *out = nullptr;
+  h2h_graph *h = nullptr;
+  int rc = guarded([&] {
+    GH_CHECK(H >= 1, H2H_ERR_ARG, "PartitionHeight must be >= 1");
+    GH_CHECK(C >= 1, H2H_ERR_ARG, "ChangeToGlobalHeight must be >= 1 (0 eliminates the root cell on the GPU, "
+                                  "where the reference reads out of bounds)");
+    GH_CHECK(method >= 1 && method <= 4, H2H_ERR_ARG, "partitionMethod must be 1..4");
+    h = new h2h_graph();
+    gh::Graph &g = h->g;
+    g.name = name ? name : "graph";
+    g.H_cli = H;
+    g.C = C;
+    g.threads = std::max(1, threads);
+    g.method = method;
+    gh::load_graph(g, edge, idf, cut);
+    GH_CHECK(g.C <= g.H, H2H_ERR_ARG, "ChangeToGlobalHeight exceeds the partition height");
+    check_symmetric(g);
+    check_connected(g);
+  });
+  if (rc != H2H_OK) { delete h; return rc; }
+  *out = h;
+  return H2H_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *h2h_last_error(void) { return gh::g_last_error.c_str(); }
+
+int h2h_load_files(const char *edge_file, const char *id_file, const char *cut_file, const char *graph_name,
+                   int partition_height, int change_height, int thread_num, int partition_method, h2h_graph **out) {
+  if (!edge_file || !id_file || !cut_file) { gh::set_last_error("file path is NULL"); return H2H_ERR_ARG; }
+  return load_common(edge_file, id_file, cut_file, graph_name, partition_height, change_height, thread_num,
+                     partition_method, out);
+}
+
+int h2h_load(const char *root, const char *graph_name, int partition_height, int change_height, int thread_num,
+             int partition_method, h2h_graph **out) {
+  if (!graph_name) { gh::set_last_error("graph_name is NULL"); return H2H_ERR_ARG; }
+  std::string r = root ? root : ".";
+  std::string name = graph_name;
+  std::string edge = r + "/Graph/USA/" + name + "Edge.txt";      // main.cu:262-270
+  std::string pre = r + "/Partition/" + name + "/" + gh::partition_file_prefix(partition_method);
+  return load_common(edge, pre + "ID.txt", pre + "Cut.txt", graph_name, partition_height, change_height, thread_num,
+                     partition_method, out);
+}
+
+void h2h_free(h2h_graph *g) { delete g; }
+
+int h2h_contract(h2h_graph *h, int use_gpu_contract) {
+  if (!h) { gh::set_last_error("null handle"); return H2H_ERR_ARG; }
+  return guarded([&] {
+    gh::Graph &g = h->g;
+    GH_CHECK(!g.contracted, H2H_ERR_STATE, "graph already contracted");
+    GH_CHECK(use_gpu_contract == 1, H2H_ERR_UNSUPPORTED,
+             "useGPUContract=0 selects the CPU partition contraction (partition_TD_T), which is not part of the "
+             "GPU hot path");
+    g.contract_device = use_gpu_contract;
+    gh::build_elimination_sets(g);
+    std::vector<int64_t> off;
+    std::vector<int> nbr, w;
+    if (g.H != g.C) {
+      gh::contract_partition_levels_gpu(g, off, nbr, w);
+    } else {  // main.cu:96: no partition level runs on the GPU
+      off.assign(g.n + 1, 0);
+      for (int v = 0; v < g.n; v++) off[v + 1] = g.adj_off[v + 1];
+      nbr = g.adj_v;
+      w = g.adj_w;
+      g.height.assign(g.n, 0);
+    }
+    gh::contract_global_heap(g, off, nbr, w);
+    gh::build_tree_and_rmq(g);
+    g.contracted = true;
+  });
+}
+
+int h2h_build_labels(h2h_graph *h, int parallel_fine, int use_gpu_construct, int label_mode) {
+  if (!h) { gh::set_last_error("null handle"); return H2H_ERR_ARG; }
+  return guarded([&] {
+    gh::Graph &g = h->g;
+    GH_CHECK(g.contracted, H2H_ERR_STATE, "h2h_contract must run before h2h_build_labels");
+    GH_CHECK(!g.labelled, H2H_ERR_STATE, "labels already built");
+    GH_CHECK(use_gpu_construct == 1, H2H_ERR_UNSUPPORTED,
+             "useGPUConstruct=0 selects the CPU label fill, which is not part of the GPU hot path");
+    GH_CHECK(parallel_fine >= 0 && parallel_fine <= 2, H2H_ERR_ARG, "parallelFine must be 0, 1 or 2");
+    GH_CHECK(label_mode == H2H_LABEL_L3 || label_mode == H2H_LABEL_L4, H2H_ERR_ARG, "label_mode must be 3 or 4");
+    g.parallel_fine = parallel_fine;
+    g.construct_device = use_gpu_construct;
+    g.label_mode = label_mode;
+    gh::allocate_labels_and_bfs(g);
+    gh::fill_labels_gpu(g);
+    gh::upload_query_index(g);
+    g.labelled = true;
+  });
+}
+
+static int single_query(const h2h_graph *h, int x, int y, int mode) {
+  if (!h) { gh::set_last_error("null handle"); return -1; }
+  int res = -1;
+  int rc = guarded([&] {
+    const gh::Graph &g = h->g;
+    GH_CHECK(g.labelled, H2H_ERR_STATE, "labels not built");
+    GH_CHECK(x >= 0 && x < g.n && y >= 0 && y < g.n, H2H_ERR_ARG, "vertex out of range");
+    int out = 0;
+    GH_CHECK(h2h_query_batch_host(h, &x, &y, &out, 1, mode) == H2H_OK, H2H_ERR_CUDA, gh::g_last_error);
+    res = out;
+  });
+  return rc == H2H_OK ? res : -1;
+}
+
+int h2h_query_lca_nohub(const h2h_graph *h, int x, int y) { return single_query(h, x, y, H2H_QUERY_LCA); }
+int h2h_query_nolca_nohub(const h2h_graph *h, int x, int y) { return single_query(h, x, y, H2H_QUERY_NOLCA); }
+
+int h2h_query_batch(const h2h_graph *h, const int *x_dev, const int *y_dev, int *out_dev, int64_t n, int mode,
+                    void *stream) {
+  if (!h) { gh::set_last_error("null handle"); return H2H_ERR_ARG; }
+  return guarded([&] {
+    const gh::Graph &g = h->g;
+    GH_CHECK(g.labelled, H2H_ERR_STATE, "labels not built");
+    GH_CHECK(mode == H2H_QUERY_LCA || mode == H2H_QUERY_NOLCA, H2H_ERR_ARG, "mode must be 0 (LCA) or 1 (noLCA)");
+    GH_CHECK(n >= 0, H2H_ERR_ARG, "negative batch size");
+    GH_CHECK(n == 0 || (x_dev && y_dev && out_dev), H2H_ERR_ARG, "null buffer");
+    gh::run_query_batch(g, x_dev, y_dev, out_dev, n, mode, (cudaStream_t)stream);
+  });
+}
+
+int h2h_query_batch_host(const h2h_graph *hc, const int *x, const int *y, int *out, int64_t n, int mode) {
+  if (!hc) { gh::set_last_error("null handle"); return H2H_ERR_ARG; }
+  h2h_graph *h = const_cast<h2h_graph *>(hc);
+  return guarded([&] {
+    const gh::Graph &g = h->g;
+    GH_CHECK(g.labelled, H2H_ERR_STATE, "labels not built");
+    GH_CHECK(mode == H2H_QUERY_LCA || mode == H2H_QUERY_NOLCA, H2H_ERR_ARG, "mode must be 0 (LCA) or 1 (noLCA)");
+    GH_CHECK(n >= 0, H2H_ERR_ARG, "negative batch size");
+    if (n == 0) return;
+    GH_CHECK(x && y && out, H2H_ERR_ARG, "null buffer");
+    for (int64_t i = 0; i < n; i++)
+      GH_CHECK(x[i] >= 0 && x[i] < g.n && y[i] >= 0 && y[i] < g.n, H2H_ERR_ARG, "vertex out of range in batch");
+    gh::HostQueryStage &s = h->stage;
+    std::lock_guard<std::mutex> lock(s.mu);
+    if (!s.stream) GH_CUDA(cudaStreamCreateWithFlags(&s.stream, cudaStreamNonBlocking));
+    if (n > s.cap) {
+      cudaFree(s.dx); cudaFree(s.dy); cudaFree(s.dout);
+      s.dx = s.dy = s.dout = nullptr;
+      s.cap = 0;
+      GH_CUDA(cudaMalloc(&s.dx, sizeof(int) * n));
+      GH_CUDA(cudaMalloc(&s.dy, sizeof(int) * n));
+      GH_CUDA(cudaMalloc(&s.dout, sizeof(int) * n));
+      s.cap = n;
+    }
+    GH_CUDA(cudaMemcpyAsync(s.dx, x, sizeof(int) * n, cudaMemcpyHostToDevice, s.stream));
+    GH_CUDA(cudaMemcpyAsync(s.dy, y, sizeof(int) * n, cudaMemcpyHostToDevice, s.stream));
+    gh::run_query_batch(g, s.dx, s.dy, s.dout, n, mode, s.stream);
+    GH_CUDA(cudaMemcpyAsync(out, s.dout, sizeof(int) * n, cudaMemcpyDeviceToHost, s.stream));
+    GH_CUDA(cudaStreamSynchronize(s.stream));
+  });
+}
+
+int h2h_get_info(const h2h_graph *h, h2h_info *info) {
+  if (!h || !info) { gh::set_last_error("null argument"); return H2H_ERR_ARG; }
+  const gh::Graph &g = h->g;
+  std::memset(info, 0, sizeof(*info));
+  const double MB = 1024.0 * 1024.0;
+  info->n = g.n;
+  info->partition_height = g.H;
+  info->change_height = g.C;
+  info->head = g.head;
+  info->tree_height = g.tree_height;
+  info->n_levels = g.tree_hash.empty() ? 0 : (int)g.tree_hash.size() - 1;
+  info->gpu_vertices = g.gpu_vertices;
+  info->label_mode = g.label_mode;
+  info->m = g.m;
+  info->label_size = g.h2h_size;
+  info->pos_size = g.pos_hash.empty() ? 0 : g.pos_hash.back();
+  info->rmq_size = (int64_t)g.rmq_id.size();
+  info->euler_size = g.euler_n;
+  info->lub_size = g.lub;
+  info->adj_size = g.x_off.empty() ? 0 : g.x_off.back();
+  info->device_bytes = g.dev.bytes;
+  info->lub_mb = (double)g.lub * 12.0 / MB;
+  info->decomposition_tree_mb = (double)g.decomposition_size * 12.0 / MB;
+  info->rmq_mb = ((double)g.rmq_hash.size() * 8 + (double)g.rmq_id.size() * 4 + (double)g.n * 4) / MB;
+  info->label_mb = ((double)(g.n + 1) * 16 + (double)info->pos_size * 4 + (double)g.h2h_size * 4) / MB;
+  const gh::Timings &t = g.t;
+  info->t_load_us = t.load;
+  info->t_rank_tree_us = t.rank_tree;
+  info->t_lub_us = t.lub;
+  info->t_translate_lub_us = t.translate_lub;
+  info->t_td_gpu_us = t.td_gpu;
+  info->t_translate_back_us = t.translate_back;
+  info->t_td_cpu_us = t.td_cpu;
+  info->t_tree_us = t.tree;
+  info->t_malloc_us = t.malloc_labels;
+  info->t_bfs_us = t.bfs;
+  info->t_translate_labels_us = t.translate_labels;
+  info->t_fill_gpu_us = t.fill_gpu;
+  info->max_label = g.max_label;
+  return H2H_OK;
+}
+
+int h2h_copy_order(const h2h_graph *h, int *order) {
+  if (!h || !order) { gh::set_last_error("null argument"); return H2H_ERR_ARG; }
+  return guarded([&] {
+    GH_CHECK(h->g.contracted, H2H_ERR_STATE, "not contracted");
+    std::copy(h->g.elim.begin(), h->g.elim.end(), order);
+  });
+}
+
+int h2h_copy_tree(const h2h_graph *h, int *father, int *depth, int *first) {
+  if (!h) { gh::set_last_error("null handle"); return H2H_ERR_ARG; }
+  return guarded([&] {
+    const gh::Graph &g = h->g;
+    GH_CHECK(g.contracted, H2H_ERR_STATE, "not contracted");
+    if (father) std::copy(g.father.begin(), g.father.end(), father);
+    if (depth) std::copy(g.depth.begin(), g.depth.end(), depth);
+    if (first) std::copy(g.first.begin(), g.first.end(), first);
+  });
+}
+
+int h2h_copy_rmq(const h2h_graph *h, int64_t *rmq_hash, int *rmq_id) {
+  if (!h) { gh::set_last_error("null handle"); return H2H_ERR_ARG; }
+  return guarded([&] {
+    const gh::Graph &g = h->g;
+    GH_CHECK(g.contracted, H2H_ERR_STATE, "not contracted");
+    if (rmq_hash) std::copy(g.rmq_hash.begin(), g.rmq_hash.end(), rmq_hash);
+    if (rmq_id) std::copy(g.rmq_id.begin(), g.rmq_id.end(), rmq_id);
+  });
+}
+
+int h2h_copy_adj(const h2h_graph *h, int64_t *adj_hash, int *adj_id, int *adj_w) {
+  if (!h) { gh::set_last_error("null handle"); return H2H_ERR_ARG; }
+  return guarded([&] {
+    const gh::Graph &g = h->g;
+    GH_CHECK(g.contracted, H2H_ERR_STATE, "not contracted");
+    if (adj_hash) std::copy(g.x_off.begin(), g.x_off.end(), adj_hash);
+    if (adj_id) std::copy(g.x_id.begin(), g.x_id.end(), adj_id);
+    if (adj_w) std::copy(g.x_w.begin(), g.x_w.end(), adj_w);
+  });
+}
+
+int h2h_copy_labels(const h2h_graph *h, int64_t *dis_hash, int *dis, int64_t *pos_hash, int *pos_id, int *pos_pos) {
+  if (!h) { gh::set_last_error("null handle"); return H2H_ERR_ARG; }
+  return guarded([&] {
+    const gh::Graph &g = h->g;
+    GH_CHECK(g.labelled, H2H_ERR_STATE, "labels not built");
+    if (dis_hash) std::copy(g.dis_hash.begin(), g.dis_hash.end(), dis_hash);
+    if (dis) gh::download_labels(g, dis);
+    if (pos_hash) std::copy(g.pos_hash.begin(), g.pos_hash.end(), pos_hash);
+    if (pos_id) std::copy(g.pos_id.begin(), g.pos_id.end(), pos_id);
+    if (pos_pos) std::copy(g.pos_pos.begin(), g.pos_pos.end(), pos_pos);
+  });
+}
+
+int h2h_copy_bfs(const h2h_graph *h, int *tree_bfs, int *tree_hash) {
+  if (!h) { gh::set_last_error("null handle"); return H2H_ERR_ARG; }
+  return guarded([&] {
+    const gh::Graph &g = h->g;
+    GH_CHECK(g.labelled, H2H_ERR_STATE, "labels not built");
+    if (tree_bfs) std::copy(g.tree_bfs.begin(), g.tree_bfs.end(), tree_bfs);
+    if (tree_hash) std::copy(g.tree_hash.begin(), g.tree_hash.end(), tree_hash);
+  });
+}
+
+int h2h_write_partition_rate(const h2h_graph *h, const char *dir) {
+  if (!h) { gh::set_last_error("null handle"); return H2H_ERR_ARG; }
+  return guarded([&] { gh::write_partition_rate(h->g, dir ? dir : "."); });
+}
+int h2h_write_contract_csv(const h2h_graph *h, const char *root) {
+  if (!h) { gh::set_last_error("null handle"); return H2H_ERR_ARG; }
+  return guarded([&] { gh::write_contract_csv(h->g, root ? root : "."); });
+}
+int h2h_write_construct_info(const h2h_graph *h, const char *root) {
+  if (!h) { gh::set_last_error("null handle"); return H2H_ERR_ARG; }
+  return guarded([&] { gh::write_construct_info(h->g, root ? root : "."); });
+}
+int h2h_write_query_result(const h2h_graph *h, const char *root, int64_t query_number, const int64_t *times_us19) {
+  if (!h) { gh::set_last_error("null handle"); return H2H_ERR_ARG; }
+  return guarded([&] { gh::write_query_result(h->g, root ? root : ".", query_number, times_us19); });
+}
+
+// ------------------------------------------------------------ tools
+
+void h2h_gen_default(h2h_gen_params *p) {
+  if (!p) return;
+  std::memset(p, 0, sizeof(*p));
+  p->n = 4096;
+  p->cols = 64;
+  p->aspect_milli = 1000;
+  p->jitter_milli = 300;
+  p->drop_permille = 100;
+  p->diag_permille = 50;
+  p->hw_k = 3;
+  p->hw_scale_milli = 400;
+  p->partition_height = 6;
+  p->seed = 20240601;
+}
+
+int h2h_generate_road(const h2h_gen_params *p, const char *root, const char *name, int64_t *n_arcs) {
+  if (!p || !root || !name) { gh::set_last_error("null argument"); return H2H_ERR_ARG; }
+  return guarded([&] { gh::generate_road(*p, root, name, n_arcs); });
+}
+
+int h2h_gen_uniform_pairs(int n_vertices, int64_t n, uint64_t seed, int *x, int *y) {
+  if (n_vertices <= 0 || n < 0 || (n > 0 && (!x || !y))) { gh::set_last_error("bad argument"); return H2H_ERR_ARG; }
+  gh::gen_uniform_pairs(n_vertices, n, seed, x, y);
+  return H2H_OK;
+}
+
+int h2h_gen_local_pairs(const h2h_graph *h, int64_t n, int max_hops, uint64_t seed, int *x, int *y) {
+  if (!h || n < 0 || (n > 0 && (!x || !y))) { gh::set_last_error("bad argument"); return H2H_ERR_ARG; }
+  gh::gen_local_pairs(h->g, n, max_hops, seed, x, y);
+  return H2H_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,54 @@
+// common.h -- shared host-side helpers for the gpuh2h library: status codes,
+// the thread-local last-error string, CUDA error checks and a wall clock.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <chrono>
+#include <cstdint>
+#include <cstdio>
+#include <stdexcept>
+#include <string>
+
+#include "gpuh2h.h"
+
+namespace gh {
+
+// Raised inside the library; capi.cpp converts it into a status code and the
+// last-error string.  Nothing crosses the C ABI as an exception.
+struct Error : std::runtime_error {
+  int code;
+  Error(int c, const std::string &m) : std::runtime_error(m), code(c) {}
+};
+
+void set_last_error(const std::string &msg);
+
+#define GH_CUDA(call)                                                                              \
+  do {                                                                                             \
+    cudaError_t e_ = (call);                                                                       \
+    if (e_ != cudaSuccess)                                                                         \
+      throw ::gh::Error(H2H_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_) + " (" + \
+                                          __FILE__ + ":" + std::to_string(__LINE__) + ")");        \
+  } while (0)
+
+#define GH_CHECK(cond, code, msg)                 \
+  do {                                            \
+    if (!(cond)) throw ::gh::Error((code), (msg)); \
+  } while (0)
+
+struct Clock {
+  std::chrono::steady_clock::time_point t0 = std::chrono::steady_clock::now();
+  void reset() { t0 = std::chrono::steady_clock::now(); }
+  // microseconds since reset, matching the reference's time_Mine (Graph_D.cuh:39-55)
+  long long us() const {
+    return std::chrono::duration_cast<std::chrono::microseconds>(std::chrono::steady_clock::now() - t0).count();
+  }
+};
+
+inline int ilog2_floor(int64_t x) {  // floor(log2(x)) for x >= 1; equals (int)log2((double)x)
+  int k = 0;
+  while ((int64_t(2) << k) <= x) k++;
+  return k;
+}
+
+}  // namespace gh

@@ -1,0 +1,116 @@
+// query.cu -- batched H2H distance queries on the device-resident index, the
+// work of H2HQuery_UsingLCA_D_noHub / H2HQuery_noLCA_D_noHub
+// (kernel_functions.cu:1143-1296) and of the host single-pair queries
+// (Query.cu:108-151).
+//
+// LCA by range minimum over the Euler tour: l, r = sorted firstAppeare,
+// k = floor(log2(r - l + 1)) (31 - clz, the integer equal of the reference's
+// (int)log2((double)...)), two sparse-table ids, the shallower wins.  Then:
+//   LCA mode:   min over p in pos(LCA) of dis[x][p] + dis[y][p]
+//   noLCA mode: min over j < depth(LCA) of dis[x][j] + dis[y][j]
+// x == y answers 0 as in the reference.
+#include <algorithm>
+#include <climits>
+
+#include "graph.h"
+
+namespace gh {
+
+namespace {
+
+template <typename T>
+T *dalloc(size_t n, int64_t &bytes) {
+  T *p = nullptr;
+  if (n == 0) n = 1;
+  cudaError_t e = cudaMalloc(&p, n * sizeof(T));
+  if (e != cudaSuccess) throw Error(H2H_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+  bytes += (int64_t)(n * sizeof(T));
+  return p;
+}
+
+struct QArgs {
+  const int *x, *y;
+  int *out;
+  int64_t n;
+  const int *first, *depth;
+  const int64_t *rmq_hash;
+  const int *rmq_id;
+  const int64_t *pos_hash;
+  const int *pos_pos;
+  const int64_t *drow;
+  const int *dis;
+};
+
+// G lanes cooperate on one query.  Every lane of the group resolves the LCA
+// (same addresses, one transaction per load), then the lanes split the min.
+template <int G, bool LCA_MODE>
+__global__ void query_kernel(QArgs A) {
+  const int lane = threadIdx.x & (G - 1);
+  const unsigned gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << ((threadIdx.x & 31) & ~(G - 1)));
+  const int64_t groups = ((int64_t)gridDim.x * blockDim.x) / G;
+  for (int64_t q = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / G; q < A.n; q += groups) {
+    const int a = __ldg(A.x + q), b = __ldg(A.y + q);
+    int res = a == b ? 0 : INT_MAX;
+    if (a != b) {
+      const int fa = __ldg(A.first + a), fb = __ldg(A.first + b);
+      const int l = min(fa, fb), r = max(fa, fb);
+      const int k = 31 - __clz(r - l + 1);
+      const int i1 = __ldg(A.rmq_id + __ldg(A.rmq_hash + l) + k);
+      const int i2 = __ldg(A.rmq_id + __ldg(A.rmq_hash + r - (1 << k) + 1) + k);
+      const int d1 = __ldg(A.depth + i1), d2 = __ldg(A.depth + i2);
+      const int *rx = A.dis + __ldg(A.drow + a);
+      const int *ry = A.dis + __ldg(A.drow + b);
+      if (LCA_MODE) {
+        const int lca = d1 <= d2 ? i1 : i2;
+        const int64_t pb = __ldg(A.pos_hash + lca), pe = __ldg(A.pos_hash + lca + 1);
+        for (int64_t t = pb + lane; t < pe; t += G) {
+          const int p = __ldg(A.pos_pos + t);
+          res = min(res, __ldg(rx + p) + __ldg(ry + p));
+        }
+      } else {
+        const int dl = min(d1, d2);
+        for (int j = lane; j < dl; j += G) res = min(res, __ldg(rx + j) + __ldg(ry + j));
+      }
+    }
+    if (G > 1) {
+      for (int o = G >> 1; o > 0; o >>= 1) res = min(res, __shfl_down_sync(gmask, res, o, G));
+    }
+    if (lane == 0) A.out[q] = res;
+  }
+}
+
+}  // namespace
+
+void upload_query_index(Graph &g) {
+  DeviceIndex &D = g.dev;
+  const int n = g.n;
+  D.euler = g.euler_n;
+  D.rmq = (int64_t)g.rmq_id.size();
+  D.first = dalloc<int>(n, D.bytes);
+  D.rmq_hash = dalloc<int64_t>(D.euler, D.bytes);
+  D.rmq_id = dalloc<int>(D.rmq, D.bytes);
+  GH_CUDA(cudaMemcpy(D.first, g.first.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
+  GH_CUDA(cudaMemcpy(D.rmq_hash, g.rmq_hash.data(), sizeof(int64_t) * D.euler, cudaMemcpyHostToDevice));
+  GH_CUDA(cudaMemcpy(D.rmq_id, g.rmq_id.data(), sizeof(int) * D.rmq, cudaMemcpyHostToDevice));
+}
+
+void run_query_batch(const Graph &g, const int *x, const int *y, int *out, int64_t n, int mode, cudaStream_t s) {
+  if (n <= 0) return;
+  const DeviceIndex &D = g.dev;
+  QArgs A{x, y, out, n, D.first, D.depth, D.rmq_hash, D.rmq_id, D.pos_hash, D.pos_pos, D.drow, D.dis};
+  static int nsm = 0;
+  if (!nsm) {
+    int dev = 0;
+    GH_CUDA(cudaGetDevice(&dev));
+    GH_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  }
+  constexpr int G = 8;
+  const int threads = 256;
+  int64_t want = (n * G + threads - 1) / threads;
+  int blocks = (int)std::min<int64_t>(want, (int64_t)nsm * 32);
+  if (mode == H2H_QUERY_LCA) query_kernel<G, true><<<std::max(1, blocks), threads, 0, s>>>(A);
+  else query_kernel<G, false><<<std::max(1, blocks), threads, 0, s>>>(A);
+  GH_CUDA(cudaGetLastError());
+}
+
+}  // namespace gh

@@ -1,0 +1,164 @@
+// tree.cpp -- tree decomposition structure and label layout on the host:
+//   getrank / getTreeStructure / makeOULAAndRMQ / OULADFS (TreeStructure.cu:102-262)
+//   mallocH2HLabel_noHub (H2HConsturction.cu:618-722)
+//   constructBFSTree     (H2HConsturction.cu:324-377)
+//
+// The Euler tour is walked with an explicit stack (the reference recurses),
+// children in increasing id order as Childs lists them.  The sparse table is
+// built directly in the reference's compacted form: row i keeps levels
+// 0..floor(log2(L - i)) (exactly the entries the reference's dense table
+// fills with a valid depth before it compacts at the first unfilled one), and
+// ties keep the left entry (`<=`, TreeStructure.cu:218).
+#include <algorithm>
+#include <atomic>
+
+#include "graph.h"
+#include "pool.h"
+
+namespace gh {
+
+void build_tree_and_rmq(Graph &g) {
+  Clock clk;
+  const int n = g.n;
+  std::vector<int> rank(n, -1);
+  for (int i = 0; i < n; i++) rank[g.elim[i]] = i;
+  g.head = g.elim[n - 1];
+  g.father.assign(n, -1);
+  for (int v = 0; v < n; v++) {
+    int best = INT32_MAX, f = -1;
+    for (int64_t k = g.x_off[v]; k < g.x_off[v + 1]; k++) {
+      int a = g.x_id[k];
+      if (rank[a] < best) { best = rank[a]; f = a; }
+    }
+    g.father[v] = f;
+  }
+  std::vector<int> cnt(n, 0);
+  for (int v = 0; v < n; v++) if (g.father[v] >= 0) cnt[g.father[v]]++;
+  g.child_off.assign(n + 1, 0);
+  for (int v = 0; v < n; v++) g.child_off[v + 1] = g.child_off[v] + cnt[v];
+  g.childs.assign(std::max(0, n - 1), -1);
+  std::vector<int> fill(g.child_off.begin(), g.child_off.end() - 1);
+  for (int v = 0; v < n; v++) if (g.father[v] >= 0) g.childs[fill[g.father[v]]++] = v;
+  GH_CHECK(g.child_off[n] == n - 1, H2H_ERR_STATE, "decomposition is not a single tree");
+  // Euler tour
+  const int64_t L = 2 * (int64_t)n - 1;
+  std::vector<int> eid(L), edep(L);
+  g.first.assign(n, -1);
+  g.depth.assign(n, -1);
+  std::vector<int> stk, cur;
+  stk.reserve(1024);
+  cur.reserve(1024);
+  int64_t e = 0;
+  g.h2h_size = 0;
+  g.tree_height = 0;
+  stk.push_back(g.head);
+  cur.push_back(0);
+  eid[e] = g.head; edep[e] = 1; g.first[g.head] = 0; e++;
+  g.depth[g.head] = 1;
+  g.h2h_size = 1;
+  g.tree_height = 1;
+  while (!stk.empty()) {
+    int v = stk.back();
+    int &c = cur.back();
+    if (g.child_off[v] + c < g.child_off[v + 1]) {
+      int ch = g.childs[g.child_off[v] + c];
+      c++;
+      int d = (int)stk.size() + 1;
+      eid[e] = ch; edep[e] = d; g.first[ch] = (int)e; e++;
+      g.depth[ch] = d;
+      g.h2h_size += d;
+      g.tree_height = std::max(g.tree_height, d);
+      stk.push_back(ch);
+      cur.push_back(0);
+    } else {
+      stk.pop_back();
+      cur.pop_back();
+      if (!stk.empty()) { eid[e] = stk.back(); edep[e] = (int)stk.size(); e++; }
+    }
+  }
+  GH_CHECK(e == L, H2H_ERR_STATE, "Euler tour does not cover the tree");
+  g.euler_n = L;
+  // compacted sparse table
+  g.rmq_hash.resize(L);
+  int64_t tot = 0;
+  for (int64_t i = 0; i < L; i++) { g.rmq_hash[i] = tot; tot += ilog2_floor(L - i) + 1; }
+  g.rmq_id.resize(tot);
+  Pool pool(g.threads);
+  std::vector<int> prev(eid), nxt(L);
+  pool.parallel_for(L, 1 << 16, [&](int64_t b, int64_t en, int) {
+    for (int64_t i = b; i < en; i++) g.rmq_id[g.rmq_hash[i]] = eid[i];
+  });
+  const int levels = ilog2_floor(L);
+  for (int j = 1; j <= levels; j++) {
+    const int64_t half = int64_t(1) << (j - 1);
+    const int64_t cnt_j = L - (int64_t(1) << j) + 1;  // rows with i + 2^j - 1 < L
+    pool.parallel_for(cnt_j, 1 << 16, [&](int64_t b, int64_t en, int) {
+      for (int64_t i = b; i < en; i++) {
+        int a = prev[i], c = prev[i + half];
+        int r = g.depth[a] <= g.depth[c] ? a : c;
+        nxt[i] = r;
+        g.rmq_id[g.rmq_hash[i] + j] = r;
+      }
+    });
+    prev.swap(nxt);
+  }
+  g.t.tree = clk.us();
+}
+
+void allocate_labels_and_bfs(Graph &g) {
+  Clock clk;
+  const int n = g.n;
+  g.dis_hash.assign(n + 1, 0);
+  g.pos_hash.assign(n + 1, 0);
+  for (int v = 0; v < n; v++) {
+    g.dis_hash[v + 1] = g.dis_hash[v] + g.depth[v];
+    g.pos_hash[v + 1] = g.pos_hash[v] + (g.x_off[v + 1] - g.x_off[v]) + 1;
+  }
+  g.pos_id.resize(g.pos_hash[n]);
+  g.pos_pos.resize(g.pos_hash[n]);
+  g.pos_w.resize(g.pos_hash[n]);
+  Pool pool(g.threads);
+  std::atomic<int> bad{-1};
+  pool.parallel_for(n, 1024, [&](int64_t b, int64_t e, int) {
+    std::vector<std::pair<int64_t, int>> tmp;
+    for (int64_t vv = b; vv < e; vv++) {
+      const int v = (int)vv;
+      const int d = g.depth[v];
+      tmp.clear();
+      for (int64_t k = g.x_off[v]; k < g.x_off[v + 1]; k++) {
+        int a = g.x_id[k], p = g.depth[a] - 1;
+        if (p < 0 || p >= d - 1) { bad = v; continue; }
+        tmp.push_back({(int64_t)p << 32 | (uint32_t)a, g.x_w[k]});
+      }
+      tmp.push_back({(int64_t)(d - 1) << 32 | (uint32_t)v, 0});
+      std::sort(tmp.begin(), tmp.end());  // positions are distinct
+      int64_t o = g.pos_hash[v];
+      for (size_t k = 0; k < tmp.size(); k++) {
+        g.pos_pos[o + k] = (int)(tmp[k].first >> 32);
+        g.pos_id[o + k] = (int)(tmp[k].first & 0xffffffff);
+        g.pos_w[o + k] = tmp[k].second;
+      }
+    }
+  });
+  GH_CHECK(bad.load() < 0, H2H_ERR_STATE, "an upper neighbour is not an ancestor in the tree");
+  g.t.malloc_labels = clk.us();
+  clk.reset();
+  // level order from the head, children in Childs order
+  g.tree_bfs.clear();
+  g.tree_bfs.reserve(n);
+  g.tree_hash.assign(1, 0);
+  g.tree_bfs.push_back(g.head);
+  g.tree_hash.push_back(1);
+  size_t qh = 0;
+  while (qh < g.tree_bfs.size()) {
+    size_t end = g.tree_bfs.size();
+    for (; qh < end; qh++) {
+      int v = g.tree_bfs[qh];
+      for (int k = g.child_off[v]; k < g.child_off[v + 1]; k++) g.tree_bfs.push_back(g.childs[k]);
+    }
+    if (g.tree_bfs.size() > end) g.tree_hash.push_back((int)g.tree_bfs.size());
+  }
+  g.t.bfs = clk.us();
+}
+
+}  // namespace gh

@@ -1,0 +1,307 @@
+"""gpuh2h -- Python mirror of the GPU-H2H operator interface over the C ABI.
+
+The reference drives its hot path through Graph_D_H::Graph members called
+from main.cu; `Graph` below keeps those names (contraction_noHub,
+constructLabel_noHub, H2HDistancQuery_UsingLCA_noHub, ...) and their argument
+meaning, and calls libgpuh2h.so (include/gpuh2h.h).  Device work needs the
+CUDA build of the library; there is no CPU fallback: every compute call
+raises if the library or a GPU is missing.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import _build
+
+H2H_OK = 0
+LABEL_L3, LABEL_L4 = 3, 4
+QUERY_LCA, QUERY_NOLCA = 0, 1
+ERRORS = {-1: "ARG", -2: "IO", -3: "FORMAT", -4: "STATE", -5: "CUDA", -6: "NOMEM", -7: "UNSUPPORTED", -8: "DEVICE"}
+
+
+class H2HError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__("%s (%d): %s" % (ERRORS.get(code, "?"), code, msg))
+        self.code = code
+
+
+class _Info(C.Structure):
+    _fields_ = [(f, C.c_int32) for f in ("n", "partition_height", "change_height", "head", "tree_height",
+                                          "n_levels", "gpu_vertices", "label_mode")] + \
+               [(f, C.c_int64) for f in ("m", "label_size", "pos_size", "rmq_size", "euler_size", "lub_size",
+                                          "adj_size", "device_bytes")] + \
+               [(f, C.c_double) for f in ("lub_mb", "decomposition_tree_mb", "rmq_mb", "label_mb")] + \
+               [(f, C.c_int64) for f in ("t_load_us", "t_rank_tree_us", "t_lub_us", "t_translate_lub_us",
+                                          "t_td_gpu_us", "t_translate_back_us", "t_td_cpu_us", "t_tree_us",
+                                          "t_malloc_us", "t_bfs_us", "t_translate_labels_us", "t_fill_gpu_us",
+                                          "max_label")]
+
+
+class GenParams(C.Structure):
+    _fields_ = [("n", C.c_int64), ("cols", C.c_int32), ("aspect_milli", C.c_int32), ("jitter_milli", C.c_int32),
+                ("drop_permille", C.c_int32), ("target_arcs", C.c_int64), ("diag_permille", C.c_int32),
+                ("hw_tiers", C.c_int32), ("hw_permille10", C.c_int32), ("hw_k", C.c_int32),
+                ("hw_scale_milli", C.c_int32), ("weight_max", C.c_int32), ("partition_height", C.c_int32),
+                ("seed", C.c_uint64)]
+
+
+# Exported symbols and their ctypes signatures (kept in step with include/*.h).
+_vp, _i32, _i64, _cp = C.c_void_p, C.c_int, C.c_int64, C.c_char_p
+SIGNATURES = {
+    "h2h_load": (_i32, [_cp, _cp, _i32, _i32, _i32, _i32, C.POINTER(_vp)]),
+    "h2h_load_files": (_i32, [_cp, _cp, _cp, _cp, _i32, _i32, _i32, _i32, C.POINTER(_vp)]),
+    "h2h_free": (None, [_vp]),
+    "h2h_last_error": (_cp, []),
+    "h2h_contract": (_i32, [_vp, _i32]),
+    "h2h_build_labels": (_i32, [_vp, _i32, _i32, _i32]),
+    "h2h_query_lca_nohub": (_i32, [_vp, _i32, _i32]),
+    "h2h_query_nolca_nohub": (_i32, [_vp, _i32, _i32]),
+    "h2h_query_batch": (_i32, [_vp, _vp, _vp, _vp, _i64, _i32, _vp]),
+    "h2h_query_batch_host": (_i32, [_vp, _vp, _vp, _vp, _i64, _i32]),
+    "h2h_get_info": (_i32, [_vp, C.POINTER(_Info)]),
+    "h2h_copy_order": (_i32, [_vp, _vp]),
+    "h2h_copy_tree": (_i32, [_vp, _vp, _vp, _vp]),
+    "h2h_copy_rmq": (_i32, [_vp, _vp, _vp]),
+    "h2h_copy_adj": (_i32, [_vp, _vp, _vp, _vp]),
+    "h2h_copy_labels": (_i32, [_vp, _vp, _vp, _vp, _vp, _vp]),
+    "h2h_copy_bfs": (_i32, [_vp, _vp, _vp]),
+    "h2h_write_partition_rate": (_i32, [_vp, _cp]),
+    "h2h_write_contract_csv": (_i32, [_vp, _cp]),
+    "h2h_write_construct_info": (_i32, [_vp, _cp]),
+    "h2h_write_query_result": (_i32, [_vp, _cp, _i64, _vp]),
+    "h2h_gen_default": (None, [C.POINTER(GenParams)]),
+    "h2h_generate_road": (_i32, [C.POINTER(GenParams), _cp, _cp, C.POINTER(_i64)]),
+    "h2h_gen_uniform_pairs": (_i32, [_i32, _i64, C.c_uint64, _vp, _vp]),
+    "h2h_gen_local_pairs": (_i32, [_vp, _i64, _i32, C.c_uint64, _vp, _vp]),
+}
+
+_lib = None
+
+
+def lib_path() -> str:
+    return _build.LIB
+
+
+def load_library(build: bool = True):
+    """Load libgpuh2h.so (building it first when `build`)."""
+    global _lib
+    if _lib is None:
+        path = _build.build() if build else _build.LIB
+        if not os.path.exists(path):
+            raise OSError("libgpuh2h.so is not built (%s)" % path)
+        L = C.CDLL(path)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _check(rc: int):
+    if rc != H2H_OK:
+        raise H2HError(rc, load_library().h2h_last_error().decode())
+
+
+def _p(a: np.ndarray):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def _require_gpu():
+    try:
+        import torch
+        ok = torch.cuda.is_available()
+    except Exception:  # torch is plumbing only; the library itself does not need it
+        ok = True
+    if not ok:
+        raise H2HError(-5, "no CUDA device: the GPU hot path has no CPU fallback")
+
+
+PARTITION_PREFIX = {1: "Latitude", 2: "Minimum", 3: "metis", 4: "scotch"}
+
+
+class Graph:
+    """One road graph through the hot path, mirroring Graph_D_H::Graph.
+
+    Graph(graphName, TreeHeight, changeHeight, threadNum, partitionMethod,
+    root=".") loads <root>/Graph/USA/<G>Edge.txt and the partition files the
+    same way main.cu:262-296 builds the paths.
+    """
+
+    def __init__(self, graphName: str, TreeHeight: int, changeHeight: int, threadNum: int = 8,
+                 partitionMethod: int = 1, root: str = ".", files: tuple | None = None):
+        L = load_library()
+        self._L = L
+        h = C.c_void_p()
+        if files is not None:
+            edge, idf, cut = files
+            rc = L.h2h_load_files(edge.encode(), idf.encode(), cut.encode(), graphName.encode(), TreeHeight,
+                                  changeHeight, threadNum, partitionMethod, C.byref(h))
+        else:
+            rc = L.h2h_load(root.encode(), graphName.encode(), TreeHeight, changeHeight, threadNum,
+                            partitionMethod, C.byref(h))
+        _check(rc)
+        self.h = h
+        self.graphName = graphName
+
+    def close(self):
+        if getattr(self, "h", None):
+            self._L.h2h_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # main.cu:149-158
+    def contraction_noHub(self, contractDevice: int = 1):
+        _require_gpu()
+        _check(self._L.h2h_contract(self.h, contractDevice))
+        return self
+
+    # main.cu:160-188
+    def constructLabel_noHub(self, parallelFine: int = 2, constructDevice: int = 1, label_mode: int = LABEL_L4):
+        _require_gpu()
+        _check(self._L.h2h_build_labels(self.h, parallelFine, constructDevice, label_mode))
+        return self
+
+    # Query.cu:108 / :124
+    def H2HDistancQuery_UsingLCA_noHub(self, x: int, y: int) -> int:
+        r = self._L.h2h_query_lca_nohub(self.h, int(x), int(y))
+        if r < 0:
+            raise H2HError(-1, self._L.h2h_last_error().decode())
+        return r
+
+    def H2HDistancQuery_noLCA_noHub(self, x: int, y: int) -> int:
+        r = self._L.h2h_query_nolca_nohub(self.h, int(x), int(y))
+        if r < 0:
+            raise H2HError(-1, self._L.h2h_last_error().decode())
+        return r
+
+    # kernel_functions.cuh:94-127 over host arrays (copies in, kernel, copies out)
+    def query(self, x, y, mode: int = QUERY_LCA) -> np.ndarray:
+        x = np.ascontiguousarray(x, np.int32)
+        y = np.ascontiguousarray(y, np.int32)
+        out = np.empty(len(x), np.int32)
+        _check(self._L.h2h_query_batch_host(self.h, _p(x), _p(y), _p(out), len(x), mode))
+        return out
+
+    def H2HQuery_UsingLCA_noHub(self, x_ptr: int, y_ptr: int, out_ptr: int, n: int, stream: int = 0):
+        """Device-pointer batch on a caller stream (torch tensors: .data_ptr(), stream.cuda_stream)."""
+        _check(self._L.h2h_query_batch(self.h, x_ptr, y_ptr, out_ptr, n, QUERY_LCA, stream or None))
+
+    def H2HQuery_noLCA_noHub(self, x_ptr: int, y_ptr: int, out_ptr: int, n: int, stream: int = 0):
+        _check(self._L.h2h_query_batch(self.h, x_ptr, y_ptr, out_ptr, n, QUERY_NOLCA, stream or None))
+
+    def query_device(self, x_ptr: int, y_ptr: int, out_ptr: int, n: int, mode: int = QUERY_LCA, stream: int = 0):
+        _check(self._L.h2h_query_batch(self.h, x_ptr, y_ptr, out_ptr, n, mode, stream or None))
+
+    # ---- accessors for parity tests
+    def info(self) -> dict:
+        inf = _Info()
+        _check(self._L.h2h_get_info(self.h, C.byref(inf)))
+        return {f: getattr(inf, f) for f, _ in _Info._fields_}
+
+    def order(self) -> np.ndarray:
+        a = np.empty(self.info()["n"], np.int32)
+        _check(self._L.h2h_copy_order(self.h, _p(a)))
+        return a
+
+    def tree(self):
+        n = self.info()["n"]
+        f, d, fi = (np.empty(n, np.int32) for _ in range(3))
+        _check(self._L.h2h_copy_tree(self.h, _p(f), _p(d), _p(fi)))
+        return f, d, fi
+
+    def rmq(self):
+        i = self.info()
+        h = np.empty(i["euler_size"], np.int64)
+        r = np.empty(i["rmq_size"], np.int32)
+        _check(self._L.h2h_copy_rmq(self.h, _p(h), _p(r)))
+        return h, r
+
+    def adj(self):
+        i = self.info()
+        ah = np.empty(i["n"] + 1, np.int64)
+        aid = np.empty(i["adj_size"], np.int32)
+        aw = np.empty(i["adj_size"], np.int32)
+        _check(self._L.h2h_copy_adj(self.h, _p(ah), _p(aid), _p(aw)))
+        return ah, aid, aw
+
+    def labels(self) -> dict:
+        i = self.info()
+        n = i["n"]
+        dh = np.empty(n + 1, np.int64)
+        dis = np.empty(i["label_size"], np.int32)
+        ph = np.empty(n + 1, np.int64)
+        pid = np.empty(i["pos_size"], np.int32)
+        pp = np.empty(i["pos_size"], np.int32)
+        _check(self._L.h2h_copy_labels(self.h, _p(dh), _p(dis), _p(ph), _p(pid), _p(pp)))
+        return dict(dis_hash=dh, dis=dis, pos_hash=ph, pos_id=pid, pos_pos=pp)
+
+    def bfs(self):
+        i = self.info()
+        tb = np.empty(i["n"], np.int32)
+        th = np.empty(i["n_levels"] + 1, np.int32)
+        _check(self._L.h2h_copy_bfs(self.h, _p(tb), _p(th)))
+        return tb, th
+
+    def local_pairs(self, n: int, max_hops: int = 20, seed: int = 1):
+        x = np.empty(n, np.int32)
+        y = np.empty(n, np.int32)
+        _check(self._L.h2h_gen_local_pairs(self.h, n, max_hops, seed, _p(x), _p(y)))
+        return x, y
+
+    # ---- CSV outputs with the reference's schemas
+    def write_partition_rate(self, directory: str = "."):
+        _check(self._L.h2h_write_partition_rate(self.h, directory.encode()))
+
+    def write_contract_csv(self, root: str = "."):
+        _check(self._L.h2h_write_contract_csv(self.h, root.encode()))
+
+    def printConstructInfo(self, root: str = "."):
+        _check(self._L.h2h_write_construct_info(self.h, root.encode()))
+
+    def write_query_result(self, root: str, query_number: int, times_us):
+        t = np.zeros(18, np.int64)
+        t[:len(times_us)] = times_us
+        _check(self._L.h2h_write_query_result(self.h, root.encode(), query_number, _p(t)))
+
+
+def gen_params(**kw) -> GenParams:
+    p = GenParams()
+    load_library().h2h_gen_default(C.byref(p))
+    for k, v in kw.items():
+        setattr(p, k, v)
+    return p
+
+
+def generate_road(root: str, name: str, **kw) -> int:
+    """Write a seeded synthetic road graph in the reference formats; returns the arc count."""
+    p = gen_params(**kw)
+    arcs = C.c_int64()
+    _check(load_library().h2h_generate_road(C.byref(p), root.encode(), name.encode(), C.byref(arcs)))
+    return arcs.value
+
+
+def uniform_pairs(n_vertices: int, n: int, seed: int = 1):
+    x = np.empty(n, np.int32)
+    y = np.empty(n, np.int32)
+    _check(load_library().h2h_gen_uniform_pairs(n_vertices, n, seed, _p(x), _p(y)))
+    return x, y
+
+
+def files_for(root: str, name: str, method: int = 1):
+    pre = os.path.join(root, "Partition", name, PARTITION_PREFIX[method])
+    return (os.path.join(root, "Graph", "USA", name + "Edge.txt"), pre + "ID.txt", pre + "Cut.txt")

@@ -1,0 +1,139 @@
+/*
+ * gpuh2h.h -- C ABI of the GB300-native GPU-H2H hot path.
+ *
+ * The reference (sauccjy/GPU-H2H) has no library interface: its operator
+ * API is the G2H command line plus the Graph_D_H::Graph members that
+ * main.cu calls and the wrappers of kernel_functions.cuh.  Each entry point
+ * below names the reference member or wrapper it stands in for (paths are
+ * relative to the reference project root).  Plain pointers and sizes only.
+ *
+ * Conventions kept from the reference:
+ *   - vertex ids are 0-based here and 1-based in Edge files;
+ *   - distances are int32, x == y gives 0, INT_MAX means "no label path";
+ *   - labels are the no-hub layout: dis_hash/pos_hash are int64 prefix
+ *     offsets, dis holds depth(v) entries per vertex (ancestor distances by
+ *     depth), pos_pos/pos_id list X(v) sorted by position.
+ * Differences, by design:
+ *   - every call returns a status (H2H_OK = 0 or a negative H2H_ERR_*) and
+ *     keeps a per-thread message for h2h_last_error(); nothing exits;
+ *   - the handle owns its host and device memory; h2h_free releases it;
+ *   - batched queries take caller-owned buffers and a caller stream.
+ */
+#ifndef GPUH2H_H
+#define GPUH2H_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define H2H_OK 0
+#define H2H_ERR_ARG (-1)         /* bad argument or out-of-range vertex          */
+#define H2H_ERR_IO (-2)          /* file missing / unreadable                    */
+#define H2H_ERR_FORMAT (-3)      /* malformed Edge / ID / Cut file               */
+#define H2H_ERR_STATE (-4)       /* call out of order (e.g. query before build)  */
+#define H2H_ERR_CUDA (-5)        /* CUDA runtime error                           */
+#define H2H_ERR_NOMEM (-6)       /* host or device allocation failed             */
+#define H2H_ERR_UNSUPPORTED (-7) /* option outside the GPU hot path              */
+#define H2H_ERR_DEVICE (-8)      /* a kernel reported an error (overflow, ...)   */
+
+#define H2H_LABEL_L3 3           /* labels as the reference ships them           */
+#define H2H_LABEL_L4 4           /* L4 father-walk enabled (exact distances)     */
+#define H2H_QUERY_LCA 0          /* H2HDistancQuery_UsingLCA_noHub semantics     */
+#define H2H_QUERY_NOLCA 1        /* H2HDistancQuery_noLCA_noHub semantics        */
+
+typedef struct h2h_graph h2h_graph;
+
+/* Graph_D_H::Graph::Graph (Graph_Fundamental.cu:4-95) with the path rules of
+ * main.cu:262-292: <root>/Graph/USA/<name>Edge.txt and
+ * <root>/Partition/<name>/{Latitude|Minimum|metis|scotch}{ID,Cut}.txt for
+ * partition_method 1/2/3/4.  root NULL means ".". */
+int h2h_load(const char *root, const char *graph_name, int partition_height, int change_height,
+             int thread_num, int partition_method, h2h_graph **out);
+
+/* The same loader with explicit file paths (Graph_Fundamental.cu:4-95). */
+int h2h_load_files(const char *edge_file, const char *id_file, const char *cut_file, const char *graph_name,
+                   int partition_height, int change_height, int thread_num, int partition_method,
+                   h2h_graph **out);
+
+/* Releases host and device memory of the handle (the reference's Graph
+ * destructor, Graph_Fundamental.cu:98-100, releases nothing). */
+void h2h_free(h2h_graph *g);
+
+/* Message of the last failing call on this thread. */
+const char *h2h_last_error(void);
+
+/* contraction_noHub (main.cu:149-158) with useGPUContract = 1:
+ * makeAdjcentNode (GraphPartition.cu:178-308), the partition levels
+ * H..C+1 on the GPU (makeCHPerHeight_2, kernel_functions.cu:520-553), the
+ * global min-degree heap for levels <= C (TDInCPU, Traditional_H2H.cu:6-25)
+ * and beforeH2H_noHub (TreeStructure.cu:41-100: ranks, tree, Euler tour,
+ * sparse table).  use_gpu_contract = 0 (the CPU partition contraction
+ * partition_TD_T) is outside the GPU hot path: H2H_ERR_UNSUPPORTED. */
+int h2h_contract(h2h_graph *g, int use_gpu_contract);
+
+/* constructLabel_noHub (main.cu:160-188): mallocH2HLabel_noHub
+ * (H2HConsturction.cu:618-722), constructBFSTree (:324-377) and the
+ * level-synchronous label fill on the GPU (makeH2HLabel_noHub_noComm_3,
+ * tanslate.cu:511-617, for parallel_fine = 2; the PF form for 0 and 1
+ * computes the same values).  label_mode is H2H_LABEL_L4 or H2H_LABEL_L3.
+ * use_gpu_construct = 0 (CPU label fill) is H2H_ERR_UNSUPPORTED. */
+int h2h_build_labels(h2h_graph *g, int parallel_fine, int use_gpu_construct, int label_mode);
+
+/* Graph::H2HDistancQuery_UsingLCA_noHub (Query.cu:108-122), one pair, on the
+ * device-resident index.  Returns the distance, or -1 on error. */
+int h2h_query_lca_nohub(const h2h_graph *g, int x, int y);
+
+/* Graph::H2HDistancQuery_noLCA_noHub (Query.cu:124-151), one pair. */
+int h2h_query_nolca_nohub(const h2h_graph *g, int x, int y);
+
+/* H2HQuery_UsingLCA_noHub / H2HQuery_noLCA_noHub (kernel_functions.cuh:94-127):
+ * n pairs from device buffers x, y into device buffer out, enqueued on the
+ * caller's cudaStream_t (NULL = legacy default stream); does not synchronize.
+ * The reference wrappers return elapsed microseconds; time with events on
+ * the same stream instead. */
+int h2h_query_batch(const h2h_graph *g, const int *x_dev, const int *y_dev, int *out_dev, int64_t n,
+                    int mode, void *stream);
+
+/* The same from host buffers: copies x, y to the device, runs the batch and
+ * copies the answers back before returning (the Query_noHub flow,
+ * main.cu:218-240: translateQuery, kernel, translateQueryResultBack). */
+int h2h_query_batch_host(const h2h_graph *g, const int *x, const int *y, int *out, int64_t n, int mode);
+
+/* Sizes and per-phase times of a built index (the printConstructInfo columns,
+ * Graph_Fundamental.cu:132-170, plus device sizes). Times in microseconds. */
+typedef struct {
+  int32_t n, partition_height, change_height, head, tree_height, n_levels, gpu_vertices, label_mode;
+  int64_t m, label_size, pos_size, rmq_size, euler_size, lub_size, adj_size;
+  int64_t device_bytes;               /* resident index bytes on the GPU           */
+  double lub_mb, decomposition_tree_mb, rmq_mb, label_mb;
+  int64_t t_load_us, t_rank_tree_us, t_lub_us, t_translate_lub_us, t_td_gpu_us, t_translate_back_us,
+      t_td_cpu_us, t_tree_us, t_malloc_us, t_bfs_us, t_translate_labels_us, t_fill_gpu_us;
+  int64_t max_label;                  /* largest finite label value               */
+} h2h_info;
+int h2h_get_info(const h2h_graph *g, h2h_info *info);
+
+/* Parity accessors (copies into caller buffers sized from h2h_info). */
+int h2h_copy_order(const h2h_graph *g, int *order);                 /* nonAdjcentNode[i].second      */
+int h2h_copy_tree(const h2h_graph *g, int *father, int *depth, int *first); /* father, H2H_TreeHeight_Hash, firstAppeare */
+int h2h_copy_rmq(const h2h_graph *g, int64_t *rmq_hash, int *rmq_id);      /* RMQHash, RMQ_ID       */
+int h2h_copy_adj(const h2h_graph *g, int64_t *adj_hash, int *adj_id, int *adj_w); /* X(v)\{v} by id  */
+int h2h_copy_labels(const h2h_graph *g, int64_t *dis_hash, int *dis, int64_t *pos_hash, int *pos_id,
+                    int *pos_pos);                                     /* H2H_* no-hub arrays          */
+int h2h_copy_bfs(const h2h_graph *g, int *tree_bfs, int *tree_hash);  /* TreeBFS, TreeHash             */
+
+/* CSV outputs with the reference's headers and columns:
+ *   <dir>/<Method>PartitionRate.csv          GraphPartition.cu:252-265
+ *   <root>/ConstructInfo/<name>/contract.csv TreeStructure.cu:54-99
+ *   <root>/ConstructInfo/<name>/constructInfo.csv Graph_Fundamental.cu:132-170
+ *   <root>/QueryResult/<name>/random.csv     Query.cu:597-622 (times in us,
+ *   19 timing columns in the reference order; unmeasured columns are 0). */
+int h2h_write_partition_rate(const h2h_graph *g, const char *dir);
+int h2h_write_contract_csv(const h2h_graph *g, const char *root);
+int h2h_write_construct_info(const h2h_graph *g, const char *root);
+int h2h_write_query_result(const h2h_graph *g, const char *root, int64_t query_number, const int64_t *times_us19);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GPUH2H_H */

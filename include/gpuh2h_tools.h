@@ -1,0 +1,53 @@
+/*
+ * gpuh2h_tools.h -- workload helpers that have no counterpart in the
+ * reference: a seeded synthetic road-graph generator that writes the
+ * reference's Edge / Node / ID / Cut formats, and seeded query-pair
+ * generators.  All arithmetic is integer, so every machine writes the same
+ * bytes for the same parameters.
+ */
+#ifndef GPUH2H_TOOLS_H
+#define GPUH2H_TOOLS_H
+#include <stdint.h>
+
+#include "gpuh2h.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct {
+  int64_t n;              /* vertices (grid filled row-major, last row partial)       */
+  int32_t cols;           /* grid columns; 0 = derived from n and aspect_milli         */
+  int32_t aspect_milli;   /* rows/cols * 1000 (1000 = square, 1300 = 1:1.3)            */
+  int32_t jitter_milli;   /* +- jitter of each point in 1/1000 cell (300 = +-0.3)      */
+  int32_t drop_permille;  /* grid edges dropped, keeping the graph connected           */
+  int64_t target_arcs;    /* if > 0, overrides drop_permille to approach this arc count */
+  int32_t diag_permille;  /* grid squares that get one diagonal                        */
+  int32_t hw_tiers;       /* highway tiers (0 = none)                                  */
+  int32_t hw_permille10;  /* tier-1 highway vertices in 1/10000 of n (50 = 0.5%)       */
+  int32_t hw_k;           /* links from each highway vertex to its k nearest peers     */
+  int32_t hw_scale_milli; /* tier-1 weight scale in 1/1000 (400 = 0.4x)                */
+  int32_t weight_max;     /* clamp weights to [1, weight_max]; 0 = no clamp            */
+  int32_t partition_height; /* latitude/longitude median bisection height             */
+  uint64_t seed;
+} h2h_gen_params;
+
+/* Fills p with the defaults of the 64x64 test grid (4,096 vertices). */
+void h2h_gen_default(h2h_gen_params *p);
+
+/* Writes <root>/Graph/USA/<name>{Edge,Node}.txt and
+ * <root>/Partition/<name>/Latitude{ID,Cut}.txt.  Returns H2H_OK or an error;
+ * *n_arcs receives the arc count written (both directions). */
+int h2h_generate_road(const h2h_gen_params *p, const char *root, const char *name, int64_t *n_arcs);
+
+/* n uniform pairs over [0, n_vertices), seeded. */
+int h2h_gen_uniform_pairs(int n_vertices, int64_t n, uint64_t seed, int *x, int *y);
+
+/* n "local" pairs: t is the end of a random walk of 1..max_hops steps from a
+ * uniform s over the loaded graph's arcs, so t lies within max_hops hops. */
+int h2h_gen_local_pairs(const h2h_graph *g, int64_t n, int max_hops, uint64_t seed, int *x, int *y);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,206 @@
+"""ctypes binding of the C oracle (h2h_oracle.c) and the reference harness.
+
+TEST INFRASTRUCTURE ONLY.  Imported by tests/, __graft_entry__.smoke() and
+bench.py's cpu_baseline / reference arm, never by the product package.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD = os.path.join(HERE, "_build")
+LIB = os.path.join(BUILD, "liboracle.so")
+REF_DIR = os.path.join(HERE, "_ref")
+
+
+def build(force: bool = False) -> str:
+    """Compile h2h_oracle.c into oracle/_build/liboracle.so (gcc, plain C)."""
+    src = os.path.join(HERE, "h2h_oracle.c")
+    hdr = os.path.join(HERE, "h2h_oracle.h")
+    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= max(
+            os.path.getmtime(src), os.path.getmtime(hdr)):
+        return LIB
+    os.makedirs(BUILD, exist_ok=True)
+    tmp = LIB + ".tmp%d" % os.getpid()
+    subprocess.check_call(["gcc", "-std=c11", "-O2", "-fPIC", "-shared", "-o", tmp, src, "-lpthread"])
+    os.replace(tmp, LIB)
+    return LIB
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        L = C.CDLL(build())
+        vp, i32, i64 = C.c_void_p, C.c_int, C.c_int64
+        L.or_load.restype = vp
+        L.or_load.argtypes = [C.c_char_p, C.c_char_p, C.c_char_p, i32, i32, i32]
+        L.or_free.argtypes = [vp]
+        L.or_error.restype = C.c_char_p
+        L.or_error.argtypes = [vp]
+        L.or_contract.argtypes = [vp]
+        L.or_build_labels.argtypes = [vp, i32, i32]
+        L.or_query_lca.argtypes = [vp, i32, i32]
+        L.or_query_nolca.argtypes = [vp, i32, i32]
+        L.or_query_batch.argtypes = [vp, vp, vp, vp, i64, i32, i32]
+        L.or_dijkstra.argtypes = [vp, i32, vp]
+        for name in ("or_n", "or_tree_height", "or_n_levels", "or_head", "or_gpu_vertices"):
+            getattr(L, name).argtypes = [vp]
+            getattr(L, name).restype = i32
+        for name in ("or_label_size", "or_pos_size", "or_rmq_size", "or_euler_size", "or_lub_size",
+                     "or_adj_total"):
+            getattr(L, name).argtypes = [vp]
+            getattr(L, name).restype = i64
+        for name in ("or_get_order", "or_get_father", "or_get_depth", "or_get_first"):
+            getattr(L, name).argtypes = [vp, vp]
+        L.or_get_rmq.argtypes = [vp, vp, vp]
+        L.or_get_labels.argtypes = [vp, vp, vp, vp, vp, vp]
+        L.or_get_bfs.argtypes = [vp, vp, vp]
+        L.or_get_adj.argtypes = [vp, vp, vp, vp]
+        _lib = L
+    return _lib
+
+
+def _p(a: np.ndarray):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+class OracleGraph:
+    """The reference pipeline restated on the CPU: load, GPU-hybrid
+    contraction (restated kernel + global heap), tree/RMQ, labels, queries."""
+
+    def __init__(self, edge: str, idf: str, cut: str, H: int, Cg: int, threads: int = 4):
+        L = lib()
+        self._L = L
+        self.h = L.or_load(edge.encode(), idf.encode(), cut.encode(), H, Cg, threads)
+        if not self.h:
+            raise IOError("oracle could not load %s / %s / %s" % (edge, idf, cut))
+        self.threads = threads
+
+    def close(self):
+        if self.h:
+            self._L.or_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def contract(self):
+        if self._L.or_contract(self.h) != 0:
+            raise RuntimeError(self._L.or_error(self.h).decode())
+        return self
+
+    def build_labels(self, l4: bool = True, threads: int | None = None):
+        if self._L.or_build_labels(self.h, 1 if l4 else 0, threads or self.threads) != 0:
+            raise RuntimeError(self._L.or_error(self.h).decode())
+        return self
+
+    @property
+    def n(self) -> int:
+        return self._L.or_n(self.h)
+
+    def _arr(self, fn, n, dt):
+        a = np.empty(n, dtype=dt)
+        fn(self.h, _p(a))
+        return a
+
+    def order(self):
+        return self._arr(self._L.or_get_order, self.n, np.int32)
+
+    def father(self):
+        return self._arr(self._L.or_get_father, self.n, np.int32)
+
+    def depth(self):
+        return self._arr(self._L.or_get_depth, self.n, np.int32)
+
+    def first(self):
+        return self._arr(self._L.or_get_first, self.n, np.int32)
+
+    def rmq(self):
+        L = self._L
+        h = np.empty(L.or_euler_size(self.h), dtype=np.int64)
+        i = np.empty(L.or_rmq_size(self.h), dtype=np.int32)
+        L.or_get_rmq(self.h, _p(h), _p(i))
+        return h, i
+
+    def labels(self):
+        L, n = self._L, self.n
+        dh = np.empty(n + 1, np.int64)
+        dis = np.empty(L.or_label_size(self.h), np.int32)
+        ph = np.empty(n + 1, np.int64)
+        pid = np.empty(L.or_pos_size(self.h), np.int32)
+        pp = np.empty(L.or_pos_size(self.h), np.int32)
+        L.or_get_labels(self.h, _p(dh), _p(dis), _p(ph), _p(pid), _p(pp))
+        return dict(dis_hash=dh, dis=dis, pos_hash=ph, pos_id=pid, pos_pos=pp)
+
+    def bfs(self):
+        L, n = self._L, self.n
+        tb = np.empty(n, np.int32)
+        th = np.empty(L.or_n_levels(self.h) + 1, np.int32)
+        L.or_get_bfs(self.h, _p(tb), _p(th))
+        return tb, th
+
+    def adj(self):
+        L, n = self._L, self.n
+        t = L.or_adj_total(self.h)
+        ah = np.empty(n + 1, np.int64)
+        aid = np.empty(t, np.int32)
+        aw = np.empty(t, np.int32)
+        L.or_get_adj(self.h, _p(ah), _p(aid), _p(aw))
+        return ah, aid, aw
+
+    def query(self, x: int, y: int, lca: bool = True) -> int:
+        return (self._L.or_query_lca if lca else self._L.or_query_nolca)(self.h, int(x), int(y))
+
+    def query_batch(self, x, y, lca: bool = True, threads: int | None = None):
+        x = np.ascontiguousarray(x, np.int32)
+        y = np.ascontiguousarray(y, np.int32)
+        out = np.empty(len(x), np.int32)
+        self._L.or_query_batch(self.h, _p(x), _p(y), _p(out), len(x), 0 if lca else 1,
+                               threads or self.threads)
+        return out
+
+    def dijkstra(self, src: int):
+        d = np.empty(self.n, np.int32)
+        self._L.or_dijkstra(self.h, int(src), _p(d))
+        return d
+
+    def summary(self) -> dict:
+        L = self._L
+        return dict(n=self.n, head=L.or_head(self.h), tree_height=L.or_tree_height(self.h),
+                    label_size=L.or_label_size(self.h), pos_size=L.or_pos_size(self.h),
+                    rmq_size=L.or_rmq_size(self.h), lub=L.or_lub_size(self.h),
+                    gpu_vertices=L.or_gpu_vertices(self.h), levels=L.or_n_levels(self.h))
+
+
+def run_reference(edge, idf, cut, H, Cg, threads=4, l4=True, pairs=None):
+    """Run the CPU build of the reference (oracle/_ref, built by build_ref.sh)
+    and return its dumped arrays.  Only available where that build exists."""
+    exe = os.path.join(REF_DIR, "ref_harness_L4" if l4 else "ref_harness_L3")
+    if not os.path.exists(exe):
+        raise FileNotFoundError(exe)
+    with tempfile.TemporaryDirectory() as wd:
+        out = os.path.join(wd, "out")
+        os.makedirs(out)
+        args = [exe, os.path.abspath(edge), os.path.abspath(idf), os.path.abspath(cut), str(H), str(Cg),
+                str(threads), out]
+        if pairs is not None:
+            pf = os.path.join(wd, "pairs.i32")
+            np.ascontiguousarray(pairs, np.int32).tofile(pf)
+            args.append(pf)
+        subprocess.run(args, cwd=wd, check=True, stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+        res = {}
+        for f in os.listdir(out):
+            name, ext = f.rsplit(".", 1)
+            res[name] = np.fromfile(os.path.join(out, f), dtype=np.int32 if ext == "i32" else np.int64)
+        return res

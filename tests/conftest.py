@@ -1,0 +1,43 @@
+import os
+import sys
+
+import numpy as np
+import pytest
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+for p in (REPO, os.path.join(REPO, "gpu-h2h_gb300")):
+    if p not in sys.path:
+        sys.path.insert(0, p)
+
+GOLDEN = os.path.join(REPO, "tests", "golden")
+SAMPLE13 = os.path.join(GOLDEN, "sample13")
+PARTS = [("Latitude", 1, 4), ("Minimum", 2, 4), ("metis", 3, 3), ("scotch", 4, 3)]
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (run with -m gpu)")
+
+
+def sample13_files(method_name):
+    return (os.path.join(SAMPLE13, "Graph", "USA", "13Edge.txt"),
+            os.path.join(SAMPLE13, "Partition", "13", method_name + "ID.txt"),
+            os.path.join(SAMPLE13, "Partition", "13", method_name + "Cut.txt"))
+
+
+@pytest.fixture(scope="session")
+def golden13():
+    return dict(np.load(os.path.join(GOLDEN, "sample13.npz")))
+
+
+@pytest.fixture(scope="session")
+def golden0():
+    return dict(np.load(os.path.join(GOLDEN, "cfg0.npz")))
+
+
+@pytest.fixture(scope="session")
+def cfg0_root(tmp_path_factory):
+    """The seeded 64x64 road-like grid (4,096 vertices, height-6 partition)."""
+    import gpuh2h
+    root = str(tmp_path_factory.mktemp("cfg0"))
+    gpuh2h.generate_road(root, "cfg0")
+    return root
