@@ -45,6 +45,21 @@ struct Clock {
   }
 };
 
+// Largest dynamic shared memory a kernel may request: the per-block opt-in
+// limit minus the kernel's own static shared memory; also raises the
+// kernel's attribute to that value.
+template <typename K>
+inline int enable_max_dynamic_smem(K kernel) {
+  int dev = 0, optin = 0;
+  GH_CUDA(cudaGetDevice(&dev));
+  GH_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  cudaFuncAttributes fa;
+  GH_CUDA(cudaFuncGetAttributes(&fa, kernel));
+  int dyn = optin - (int)fa.sharedSizeBytes;
+  GH_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
+  return dyn;
+}
+
 inline int ilog2_floor(int64_t x) {  // floor(log2(x)) for x >= 1; equals (int)log2((double)x)
   int k = 0;
   while ((int64_t(2) << k) <= x) k++;

@@ -481,12 +481,8 @@ void contract_partition_levels_gpu(Graph &g, std::vector<int64_t> &lst_off, std:
     g.t.translate_lub = clk.us();
     clk.reset();
 
-    int dev = 0;
-    GH_CUDA(cudaGetDevice(&dev));
-    int smem_optin = 0;
-    GH_CUDA(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    const int smem_dyn = enable_max_dynamic_smem(contract_level_kernel);
     const int kThreads = 256, kWarps = kThreads / 32;
-    GH_CUDA(cudaFuncSetAttribute(contract_level_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_optin));
     for (int h = g.H; h > g.C; h--) {
       const int64_t lo = (int64_t(1) << (h - 1)) - 1, hi = (int64_t(1) << h) - 2;
       const int ncell = (int)(hi - lo + 1);
@@ -519,7 +515,7 @@ void contract_partition_levels_gpu(Graph &g, std::vector<int64_t> &lst_off, std:
       int64_t keys_b = 3 * al(sizeof(int) * (int64_t)kmax);
       int64_t lists_b = al(4LL * lmax) * 2 + al(8LL * lmax) + al(4LL * lmax) * 2;
       int64_t warp_b = al(8LL * A.wbuf * kWarps) + al(4LL * A.wbuf * kWarps);
-      const int64_t budget = smem_optin - 2048;
+      const int64_t budget = smem_dyn;
       A.keys_in_smem = 1;
       A.lists_in_smem = 1;
       int64_t smem = keys_b + lists_b + warp_b;

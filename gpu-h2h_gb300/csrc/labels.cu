@@ -191,11 +191,10 @@ void fill_labels_gpu(Graph &g) {
     GH_CUDA(cudaDeviceSynchronize());
     g.t.translate_labels = clk.us();
     clk.reset();
-    int dev = 0, smem_optin = 0, nsm = 0;
+    int dev = 0, nsm = 0;
     GH_CUDA(cudaGetDevice(&dev));
-    GH_CUDA(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
     GH_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-    GH_CUDA(cudaFuncSetAttribute(fill_level_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_optin));
+    const int smem_dyn = enable_max_dynamic_smem(fill_level_kernel);
     cudaEvent_t e0, e1;
     GH_CUDA(cudaEventCreate(&e0));
     GH_CUDA(cudaEventCreate(&e1));
@@ -203,7 +202,7 @@ void fill_labels_gpu(Graph &g) {
     for (int l = 1; l < nlev; l++) {
       const int d = l + 1;
       const size_t per_warp = (size_t)((d + 3) & ~3) * 4 + (size_t)d * 8;
-      int wpb = (int)std::min<size_t>(8, (size_t)(smem_optin - 1024) / per_warp);
+      int wpb = (int)std::min<size_t>(8, (size_t)smem_dyn / per_warp);
       GH_CHECK(wpb >= 1, H2H_ERR_DEVICE, "tree too deep for the shared-memory row staging");
       const int count = g.tree_hash[l + 1] - g.tree_hash[l];
       FillArgs A;

@@ -32,6 +32,7 @@ struct QArgs {
   const int *x, *y;
   int *out;
   int64_t n;
+  int nv;  // vertices; ids outside [0, nv) answer -1 without touching the index
   const int *first, *depth;
   const int64_t *rmq_hash;
   const int *rmq_id;
@@ -50,8 +51,9 @@ __global__ void query_kernel(QArgs A) {
   const int64_t groups = ((int64_t)gridDim.x * blockDim.x) / G;
   for (int64_t q = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / G; q < A.n; q += groups) {
     const int a = __ldg(A.x + q), b = __ldg(A.y + q);
-    int res = a == b ? 0 : INT_MAX;
-    if (a != b) {
+    const bool valid = (unsigned)a < (unsigned)A.nv && (unsigned)b < (unsigned)A.nv;
+    int res = !valid ? -1 : (a == b ? 0 : INT_MAX);
+    if (valid && a != b) {
       const int fa = __ldg(A.first + a), fb = __ldg(A.first + b);
       const int l = min(fa, fb), r = max(fa, fb);
       const int k = 31 - __clz(r - l + 1);
@@ -97,7 +99,7 @@ void upload_query_index(Graph &g) {
 void run_query_batch(const Graph &g, const int *x, const int *y, int *out, int64_t n, int mode, cudaStream_t s) {
   if (n <= 0) return;
   const DeviceIndex &D = g.dev;
-  QArgs A{x, y, out, n, D.first, D.depth, D.rmq_hash, D.rmq_id, D.pos_hash, D.pos_pos, D.drow, D.dis};
+  QArgs A{x, y, out, n, g.n, D.first, D.depth, D.rmq_hash, D.rmq_id, D.pos_hash, D.pos_pos, D.drow, D.dis};
   static int nsm = 0;
   if (!nsm) {
     int dev = 0;

@@ -90,6 +90,8 @@ int h2h_query_nolca_nohub(const h2h_graph *g, int x, int y);
 /* H2HQuery_UsingLCA_noHub / H2HQuery_noLCA_noHub (kernel_functions.cuh:94-127):
  * n pairs from device buffers x, y into device buffer out, enqueued on the
  * caller's cudaStream_t (NULL = legacy default stream); does not synchronize.
+ * A pair with an id outside [0, n) answers -1 (the reference reads out of
+ * bounds there).
  * The reference wrappers return elapsed microseconds; time with events on
  * the same stream instead. */
 int h2h_query_batch(const h2h_graph *g, const int *x_dev, const int *y_dev, int *out_dev, int64_t n,
