@@ -1,0 +1,416 @@
+"""bench.py -- H2H build seconds and batched query throughput on GB300.
+
+Workload (one GPU): the synthetic road graph with the size of DIMACS NY
+(264,346 vertices, ~733,846 arcs, jittered grid on a 1:1.3 box plus a sparse
+highway layer, int32 Euclidean weights), latitude/longitude partition of
+height 10, ChangeToGlobalHeight 2, GPU contraction + GPU L4 labels.  A step is
+one batch of 2*10^6 query pairs (10^6 uniform + 10^6 local, t within 20 hops
+of s) answered in UsingLCA mode on the device-resident index.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+N>1 runs under torchrun: every rank builds its own replica of the index and
+answers its own batch (queries are independent: weak scaling, no collective
+on the data path); the timed region is bracketed by barriers and the slowest
+rank's time is reported.  `--impl reference` times the reference's CPU
+algorithm (the oracle restatement of makeH2HLabel_noHub_multiThred and the
+H2HDistancQuery_UsingLCA_noHub thread loop) on the host cores instead.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+for _p in (REPO, os.path.join(REPO, "gpu-h2h_gb300")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = json.load(open(os.path.join(REPO, "BASELINE.json")))["metric"]
+WORKLOAD = dict(name="cfg1", n=264346, target_arcs=733846, aspect_milli=1300, jitter_milli=300, diag_permille=50,
+                hw_tiers=1, hw_permille10=50, hw_k=3, hw_scale_milli=400, partition_height=10, seed=1)
+H, C = 10, 2
+Q_UNIFORM, Q_LOCAL, LOCAL_HOPS = 1_000_000, 1_000_000, 20
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def gen_graph(root: str):
+    import gpuh2h
+    kw = {k: v for k, v in WORKLOAD.items() if k != "name"}
+    kw.update(cols=0, drop_permille=0)
+    arcs = gpuh2h.generate_road(root, WORKLOAD["name"], **kw)
+    return gpuh2h.files_for(root, WORKLOAD["name"]), arcs
+
+
+def query_pairs(g, n_vertices: int, seed: int):
+    import gpuh2h
+    x, y = gpuh2h.uniform_pairs(n_vertices, Q_UNIFORM, seed)
+    lx, ly = g.local_pairs(Q_LOCAL, LOCAL_HOPS, seed + 1000)
+    return np.concatenate([x, lx]), np.concatenate([y, ly])
+
+
+def algorithmic_bytes(g, x, y) -> int:
+    """Sum over queries of 84 + 12*|pos(LCA)| bytes (UsingLCA mode): pair ids 8,
+    firstAppeare 8, RMQHash 16, RMQ_ID 8, depth 8, pos_hash 16, dis_hash 16,
+    result 4, and per LCA position 4 (pos) + 8 (two label entries)."""
+    _, depth, first = g.tree()
+    rh, ri = g.rmq()
+    ph = g.labels_pos_hash()
+    fa, fb = first[x].astype(np.int64), first[y].astype(np.int64)
+    lo, hi = np.minimum(fa, fb), np.maximum(fa, fb)
+    k = np.floor(np.log2(hi - lo + 1)).astype(np.int64)
+    i1 = ri[rh[lo] + k]
+    i2 = ri[rh[hi - (1 << k) + 1] + k]
+    lca = np.where(depth[i1] <= depth[i2], i1, i2)
+    kq = ph[lca + 1] - ph[lca]
+    same = x == y
+    return int(np.where(same, 12, 84 + 12 * kq).sum())
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled while the timed region runs."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.p = None
+
+    def start(self):
+        """Start sampling and return once the first sample is in (NVML start-up
+        stays outside the timed region)."""
+        import threading
+        self.lines = []
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                                       "-i", str(self.gpu), "-lms", "50"], stdout=subprocess.PIPE,
+                                      stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.p = None
+            return
+        first = threading.Event()
+
+        def reader():
+            for line in self.p.stdout:
+                self.lines.append(line)
+                first.set()
+            first.set()
+        self.t = threading.Thread(target=reader, daemon=True)
+        self.t.start()
+        first.wait(timeout=20)
+
+    def stop(self) -> dict:
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.1)
+        self.p.terminate()
+        self.p.wait(timeout=10)
+        self.t.join(timeout=10)
+        out = "".join(self.lines)
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.strip().splitlines():
+            f = [s.strip() for s in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, val in zip(names, f[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def reduce_max(value: float, world: int) -> float:
+    if world == 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([value], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world: int):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def build_index(files, threads: int):
+    import gpuh2h
+    t0 = time.perf_counter()
+    g = gpuh2h.Graph(WORKLOAD["name"], H, C, threads, 1, files=files)
+    g.contraction_noHub(1)
+    g.constructLabel_noHub(2, 1, gpuh2h.LABEL_L4)
+    return g, time.perf_counter() - t0
+
+
+def cpu_reference_run(files, x, y, threads: int, budget_s: float):
+    """The reference's CPU path restated (oracle): build + threaded query loop."""
+    from oracle import oracle
+    t0 = time.perf_counter()
+    o = oracle.OracleGraph(*files, H, C, threads).contract()
+    t1 = time.perf_counter()
+    o.build_labels(l4=True, threads=threads)
+    t2 = time.perf_counter()
+    done, q_time, reps = 0, 0.0, 0
+    while q_time < budget_s and reps < 50:
+        s = time.perf_counter()
+        o.query_batch(x, y, lca=True, threads=threads)
+        q_time += time.perf_counter() - s
+        done += len(x)
+        reps += 1
+    return o, dict(contract_s=t1 - t0, labels_s=t2 - t1, query_s=q_time, queries=done, reps=reps)
+
+
+def run_reference_arm(args):
+    world, rank, local = dist_setup()
+    if rank != 0:
+        return 0
+    import gpuh2h
+    threads = os.cpu_count() or 1
+    with tempfile.TemporaryDirectory(prefix="h2h_bench_") as root:
+        files, arcs = gen_graph(root)
+        # pairs from the same generator as the GPU arm (host-only helpers)
+        import ctypes
+        L = gpuh2h.load_library()
+        h = ctypes.c_void_p()
+        gpuh2h._check(L.h2h_load_files(*[f.encode() for f in files], b"cfg1", H, C, threads, 1, ctypes.byref(h)))
+        ux, uy = gpuh2h.uniform_pairs(WORKLOAD["n"], Q_UNIFORM, 7)
+        lx, ly = np.empty(Q_LOCAL, np.int32), np.empty(Q_LOCAL, np.int32)
+        gpuh2h._check(L.h2h_gen_local_pairs(h, Q_LOCAL, LOCAL_HOPS, 7 + 1000, gpuh2h._p(lx), gpuh2h._p(ly)))
+        L.h2h_free(h)
+        x, y = np.concatenate([ux, lx]), np.concatenate([uy, ly])
+        from oracle import oracle
+        t0 = time.perf_counter()
+        o = oracle.OracleGraph(*files, H, C, threads).contract()
+        t1 = time.perf_counter()
+        o.build_labels(l4=True, threads=threads)
+        t2 = time.perf_counter()
+        for _ in range(args.warmup):
+            o.query_batch(x, y, lca=True, threads=threads)
+        times = []
+        for _ in range(args.steps):
+            s = time.perf_counter()
+            o.query_batch(x, y, lca=True, threads=threads)
+            times.append(time.perf_counter() - s)
+    total = sum(times)
+    value = args.steps * len(x) / total
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "queries/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * total / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
+        "config": {"workload": "cfg1 road graph 264,346 vertices / %d arcs, H=10, C=2, L4 labels, 2e6 queries/step "
+                               "(1e6 uniform + 1e6 local)" % arcs, "parallelism": "host threads"},
+        "build_s": t2 - t0, "build_phases_s": {"contract": t1 - t0, "labels": t2 - t1},
+        "cpu_baseline": {"value": value, "unit": "queries/s", "cores": threads, "kind": "port",
+                         "sample": "%d steps x %d queries, UsingLCA, %d threads" % (args.steps, len(x), threads)},
+        "e2e": {"value": value, "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--build-reps", type=int, default=3)
+    ap.add_argument("--latency-batches", type=int, default=200)
+    ap.add_argument("--cpu-budget", type=float, default=10.0, help="seconds of CPU query work for cpu_baseline")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    if args.impl == "reference":
+        return run_reference_arm(args)
+
+    import torch
+    world, rank, local = dist_setup()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    import gpuh2h
+    threads = max(1, (os.cpu_count() or 1) // max(1, world))
+    root = tempfile.mkdtemp(prefix="h2h_bench_%d_" % rank)
+    files, arcs = gen_graph(root)
+    # ---- build (whole H2H construction from the loaded files), best-of and median
+    build_times, phases = [], None
+    g = None
+    for r in range(max(1, args.build_reps)):
+        if g is not None:
+            g.close()
+        torch.cuda.synchronize()
+        g, bt = build_index(files, threads)
+        build_times.append(bt)
+    info = g.info()
+    phases = {k[2:-3]: info[k] / 1e3 for k in info if k.startswith("t_") and k.endswith("_us")}
+    x, y = query_pairs(g, info["n"], 7 + rank)
+    nq = len(x)
+    xd = torch.from_numpy(x).cuda()
+    yd = torch.from_numpy(y).cuda()
+    od = torch.empty_like(xd)
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
+    for _ in range(args.warmup):
+        g.query_device(xd.data_ptr(), yd.data_ptr(), od.data_ptr(), nq, gpuh2h.QUERY_LCA, sp)
+    torch.cuda.synchronize()
+    # parity spot check of this batch against the noLCA form (both exact with L4)
+    od2 = torch.empty_like(xd)
+    g.query_device(xd.data_ptr(), yd.data_ptr(), od2.data_ptr(), nq, gpuh2h.QUERY_NOLCA, sp)
+    torch.cuda.synchronize()
+    assert torch.equal(od, od2), "UsingLCA and noLCA answers differ"
+    # ---- timed region: K steps, device-resident inputs
+    sampler = ClockSampler(local)
+    barrier(world)
+    torch.cuda.synchronize()
+    sampler.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        g.query_device(xd.data_ptr(), yd.data_ptr(), od.data_ptr(), nq, gpuh2h.QUERY_LCA, sp)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    barrier(world)
+    clocks = sampler.stop()
+    t_local = e0.elapsed_time(e1) / 1000.0
+    t_max = reduce_max(t_local, world)
+    value = world * args.steps * nq / t_max
+    kernel_s = t_local / args.steps
+    # ---- roofline of the query kernel
+    abytes = algorithmic_bytes(g, x, y)
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(REPO, "MEASURED_PEAKS.json")))
+        peak, peak_src = float(peaks["hbm_gbs"]), "measured"
+    except Exception:
+        peak, peak_src = 6800.0, "fallback"
+    achieved = abytes / kernel_s / 1e9
+    traffic = None
+    tf = os.path.join(REPO, "profiles", "query_traffic.json")
+    if os.path.exists(tf):
+        try:
+            traffic = json.load(open(tf)).get("dram_bytes_per_query")
+            traffic = traffic * nq if traffic is not None else None
+        except Exception:
+            traffic = None
+    # ---- plain GPU mapping (one thread per query, the reference's kernel layout)
+    for _ in range(3):
+        g.query_device_plain(xd.data_ptr(), yd.data_ptr(), od2.data_ptr(), nq, gpuh2h.QUERY_LCA, sp)
+    torch.cuda.synchronize()
+    p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps_plain = max(3, min(args.steps, 50))
+    p0.record(stream)
+    for _ in range(reps_plain):
+        g.query_device_plain(xd.data_ptr(), yd.data_ptr(), od2.data_ptr(), nq, gpuh2h.QUERY_LCA, sp)
+    p1.record(stream)
+    torch.cuda.synchronize()
+    plain_value = reps_plain * nq / (p0.elapsed_time(p1) / 1000.0)
+    assert torch.equal(od, od2)
+    # ---- e2e through the public host-buffer API (pinned host buffers)
+    xh = torch.from_numpy(x).pin_memory()
+    yh = torch.from_numpy(y).pin_memory()
+    oh = torch.empty(nq, dtype=torch.int32).pin_memory()
+    for _ in range(3):
+        g.query_host_ptr(xh.data_ptr(), yh.data_ptr(), oh.data_ptr(), nq, gpuh2h.QUERY_LCA)
+    barrier(world)
+    e2e_steps = max(3, min(args.steps, 50))
+    s = time.perf_counter()
+    for _ in range(e2e_steps):
+        g.query_host_ptr(xh.data_ptr(), yh.data_ptr(), oh.data_ptr(), nq, gpuh2h.QUERY_LCA)
+    e2e_local = time.perf_counter() - s
+    e2e_t = reduce_max(e2e_local, world)
+    e2e_value = world * e2e_steps * nq / e2e_t
+    assert np.array_equal(oh.numpy(), od.cpu().numpy())
+    # ---- latency of 10^5-query batches (device-only and through the host API)
+    bq = 100_000
+    lat_dev, lat_e2e = [], []
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.latency_batches)]
+    for i, (a, b) in enumerate(ev):
+        off = (i * bq) % (nq - bq)
+        a.record(stream)
+        g.query_device(xd.data_ptr() + 4 * off, yd.data_ptr() + 4 * off, od.data_ptr() + 4 * off, bq,
+                       gpuh2h.QUERY_LCA, sp)
+        b.record(stream)
+    torch.cuda.synchronize()
+    lat_dev = [a.elapsed_time(b) * 1000.0 for a, b in ev]
+    for i in range(args.latency_batches):
+        off = (i * bq) % (nq - bq)
+        s = time.perf_counter()
+        g.query_host_ptr(xh.data_ptr() + 4 * off, yh.data_ptr() + 4 * off, oh.data_ptr() + 4 * off, bq,
+                         gpuh2h.QUERY_LCA)
+        lat_e2e.append((time.perf_counter() - s) * 1e6)
+    # ---- CPU baseline (rank 0, N=1 only): the reference's CPU algorithm on host cores
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cores = os.cpu_count() or 1
+        _, cb = cpu_reference_run(files, x, y, cores, args.cpu_budget)
+        cpu = {"value": cb["queries"] / cb["query_s"], "unit": "queries/s", "cores": cores, "kind": "port",
+               "sample": "%d x %d queries (UsingLCA, L4 labels) over %d host threads; oracle build %.1f s "
+                         "(contract %.1f s + labels %.1f s)" % (cb["reps"], nq, cores,
+                                                                 cb["contract_s"] + cb["labels_s"], cb["contract_s"],
+                                                                 cb["labels_s"]),
+               "build_s": cb["contract_s"] + cb["labels_s"]}
+    pct = lambda v, q: float(np.percentile(np.asarray(v), q))
+    line = {
+        "metric": METRIC, "value": value, "unit": "queries/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1000.0 * t_max / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
+        "config": {"workload": "cfg1 road graph 264,346 vertices / %d arcs (jittered 1:1.3 grid + highway layer), "
+                               "lat/long partition H=10, C=2, GPU contraction + GPU L4 labels; step = 2e6 queries "
+                               "(1e6 uniform + 1e6 local <=20 hops), UsingLCA" % arcs,
+                   "queries_per_step": nq, "l2": "index %.2f GB resident > L2 (no flush)" % (info["device_bytes"] / 1e9),
+                   "parallelism": "replicas x%d (queries sharded by rank)" % world},
+        "build_s": statistics.median(build_times), "build_s_min": min(build_times),
+        "build_phases_ms": phases,
+        "index": {"tree_height": info["tree_height"], "label_entries": info["label_size"],
+                  "device_bytes": info["device_bytes"], "max_label": info["max_label"]},
+        "latency_us_1e5": {"device_p50": pct(lat_dev, 50), "device_p99": pct(lat_dev, 99),
+                           "e2e_p50": pct(lat_e2e, 50), "e2e_p99": pct(lat_e2e, 99)},
+        "plain_gpu": {"value": plain_value, "unit": "queries/s", "what": "one thread per query (reference mapping)"},
+        "e2e": {"value": e2e_value, "unit": "queries/s", "h2d_bytes_per_step": 8 * nq, "d2h_bytes_per_step": 4 * nq},
+        "gpu_launches": args.steps,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": traffic, "peak_source": peak_src, "algorithmic_bytes_per_launch": abytes,
+                     "kernel": "query_kernel<8,LCA>"},
+        "clocks": clocks,
+        "cpu_baseline": cpu,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    g.close()
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

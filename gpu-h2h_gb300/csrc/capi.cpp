@@ -223,6 +223,17 @@ int h2h_query_batch(const h2h_graph *h, const int *x_dev, const int *y_dev, int 
   });
 }
 
+int h2h_query_batch_plain(const h2h_graph *h, const int *x_dev, const int *y_dev, int *out_dev, int64_t n, int mode,
+                          void *stream) {
+  if (!h) { gh::set_last_error("null handle"); return H2H_ERR_ARG; }
+  return guarded([&] {
+    GH_CHECK(h->g.labelled, H2H_ERR_STATE, "labels not built");
+    GH_CHECK(mode == H2H_QUERY_LCA || mode == H2H_QUERY_NOLCA, H2H_ERR_ARG, "mode must be 0 (LCA) or 1 (noLCA)");
+    GH_CHECK(n == 0 || (x_dev && y_dev && out_dev), H2H_ERR_ARG, "null buffer");
+    gh::run_query_batch_plain(h->g, x_dev, y_dev, out_dev, n, mode, (cudaStream_t)stream);
+  });
+}
+
 int h2h_query_batch_host(const h2h_graph *hc, const int *x, const int *y, int *out, int64_t n, int mode) {
   if (!hc) { gh::set_last_error("null handle"); return H2H_ERR_ARG; }
   h2h_graph *h = const_cast<h2h_graph *>(hc);
@@ -233,8 +244,6 @@ int h2h_query_batch_host(const h2h_graph *hc, const int *x, const int *y, int *o
     GH_CHECK(n >= 0, H2H_ERR_ARG, "negative batch size");
     if (n == 0) return;
     GH_CHECK(x && y && out, H2H_ERR_ARG, "null buffer");
-    for (int64_t i = 0; i < n; i++)
-      GH_CHECK(x[i] >= 0 && x[i] < g.n && y[i] >= 0 && y[i] < g.n, H2H_ERR_ARG, "vertex out of range in batch");
     gh::HostQueryStage &s = h->stage;
     std::lock_guard<std::mutex> lock(s.mu);
     if (!s.stream) GH_CUDA(cudaStreamCreateWithFlags(&s.stream, cudaStreamNonBlocking));
@@ -251,7 +260,14 @@ int h2h_query_batch_host(const h2h_graph *hc, const int *x, const int *y, int *o
     GH_CUDA(cudaMemcpyAsync(s.dy, y, sizeof(int) * n, cudaMemcpyHostToDevice, s.stream));
     gh::run_query_batch(g, s.dx, s.dy, s.dout, n, mode, s.stream);
     GH_CUDA(cudaMemcpyAsync(out, s.dout, sizeof(int) * n, cudaMemcpyDeviceToHost, s.stream));
+    int bad = 0;
+    GH_CUDA(cudaMemcpyAsync(&bad, g.dev.err, sizeof(int), cudaMemcpyDeviceToHost, s.stream));
     GH_CUDA(cudaStreamSynchronize(s.stream));
+    if (bad) {
+      GH_CUDA(cudaMemsetAsync(g.dev.err, 0, sizeof(int), s.stream));
+      GH_CUDA(cudaStreamSynchronize(s.stream));
+      throw gh::Error(H2H_ERR_ARG, "vertex id out of range in batch (those pairs answered -1)");
+    }
   });
 }
 

@@ -100,5 +100,7 @@ void download_labels(const Graph &g, int *dis_out);    // labels.cu, reference l
 void upload_query_index(Graph &g);                     // query.cu
 void run_query_batch(const Graph &g, const int *x, const int *y, int *out, int64_t n, int mode,
                      cudaStream_t s);                  // query.cu
+void run_query_batch_plain(const Graph &g, const int *x, const int *y, int *out, int64_t n, int mode,
+                           cudaStream_t s);                  // query.cu, one thread per query
 
 }  // namespace gh

@@ -40,6 +40,7 @@ struct QArgs {
   const int *pos_pos;
   const int64_t *drow;
   const int *dis;
+  int *bad;  // set to 1 when a pair holds an id outside [0, nv)
 };
 
 // G lanes cooperate on one query.  Every lane of the group resolves the LCA
@@ -53,6 +54,7 @@ __global__ void query_kernel(QArgs A) {
     const int a = __ldg(A.x + q), b = __ldg(A.y + q);
     const bool valid = (unsigned)a < (unsigned)A.nv && (unsigned)b < (unsigned)A.nv;
     int res = !valid ? -1 : (a == b ? 0 : INT_MAX);
+    if (!valid && lane == 0) atomicExch(A.bad, 1);
     if (valid && a != b) {
       const int fa = __ldg(A.first + a), fb = __ldg(A.first + b);
       const int l = min(fa, fb), r = max(fa, fb);
@@ -99,7 +101,7 @@ void upload_query_index(Graph &g) {
 void run_query_batch(const Graph &g, const int *x, const int *y, int *out, int64_t n, int mode, cudaStream_t s) {
   if (n <= 0) return;
   const DeviceIndex &D = g.dev;
-  QArgs A{x, y, out, n, g.n, D.first, D.depth, D.rmq_hash, D.rmq_id, D.pos_hash, D.pos_pos, D.drow, D.dis};
+  QArgs A{x, y, out, n, g.n, D.first, D.depth, D.rmq_hash, D.rmq_id, D.pos_hash, D.pos_pos, D.drow, D.dis, D.err};
   static int nsm = 0;
   if (!nsm) {
     int dev = 0;
@@ -112,6 +114,18 @@ void run_query_batch(const Graph &g, const int *x, const int *y, int *out, int64
   int blocks = (int)std::min<int64_t>(want, (int64_t)nsm * 32);
   if (mode == H2H_QUERY_LCA) query_kernel<G, true><<<std::max(1, blocks), threads, 0, s>>>(A);
   else query_kernel<G, false><<<std::max(1, blocks), threads, 0, s>>>(A);
+  GH_CUDA(cudaGetLastError());
+}
+
+void run_query_batch_plain(const Graph &g, const int *x, const int *y, int *out, int64_t n, int mode,
+                           cudaStream_t s) {
+  if (n <= 0) return;
+  const DeviceIndex &D = g.dev;
+  QArgs A{x, y, out, n, g.n, D.first, D.depth, D.rmq_hash, D.rmq_id, D.pos_hash, D.pos_pos, D.drow, D.dis, D.err};
+  const int threads = 256;
+  int blocks = (int)std::min<int64_t>((n + threads - 1) / threads, INT32_MAX);
+  if (mode == H2H_QUERY_LCA) query_kernel<1, true><<<blocks, threads, 0, s>>>(A);
+  else query_kernel<1, false><<<blocks, threads, 0, s>>>(A);
   GH_CUDA(cudaGetLastError());
 }
 

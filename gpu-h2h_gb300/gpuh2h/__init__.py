@@ -61,6 +61,7 @@ SIGNATURES = {
     "h2h_query_nolca_nohub": (_i32, [_vp, _i32, _i32]),
     "h2h_query_batch": (_i32, [_vp, _vp, _vp, _vp, _i64, _i32, _vp]),
     "h2h_query_batch_host": (_i32, [_vp, _vp, _vp, _vp, _i64, _i32]),
+    "h2h_query_batch_plain": (_i32, [_vp, _vp, _vp, _vp, _i64, _i32, _vp]),
     "h2h_get_info": (_i32, [_vp, C.POINTER(_Info)]),
     "h2h_copy_order": (_i32, [_vp, _vp]),
     "h2h_copy_tree": (_i32, [_vp, _vp, _vp, _vp]),
@@ -207,6 +208,15 @@ class Graph:
     def query_device(self, x_ptr: int, y_ptr: int, out_ptr: int, n: int, mode: int = QUERY_LCA, stream: int = 0):
         _check(self._L.h2h_query_batch(self.h, x_ptr, y_ptr, out_ptr, n, mode, stream or None))
 
+    def query_device_plain(self, x_ptr: int, y_ptr: int, out_ptr: int, n: int, mode: int = QUERY_LCA,
+                           stream: int = 0):
+        """The reference's one-thread-per-query mapping (measurement baseline)."""
+        _check(self._L.h2h_query_batch_plain(self.h, x_ptr, y_ptr, out_ptr, n, mode, stream or None))
+
+    def query_host_ptr(self, x_ptr: int, y_ptr: int, out_ptr: int, n: int, mode: int = QUERY_LCA):
+        """h2h_query_batch_host on raw host pointers (e.g. pinned torch tensors)."""
+        _check(self._L.h2h_query_batch_host(self.h, x_ptr, y_ptr, out_ptr, n, mode))
+
     # ---- accessors for parity tests
     def info(self) -> dict:
         inf = _Info()
@@ -249,6 +259,12 @@ class Graph:
         pp = np.empty(i["pos_size"], np.int32)
         _check(self._L.h2h_copy_labels(self.h, _p(dh), _p(dis), _p(ph), _p(pid), _p(pp)))
         return dict(dis_hash=dh, dis=dis, pos_hash=ph, pos_id=pid, pos_pos=pp)
+
+    def labels_pos_hash(self) -> np.ndarray:
+        """H2H_pos_hash only (no label download)."""
+        ph = np.empty(self.info()["n"] + 1, np.int64)
+        _check(self._L.h2h_copy_labels(self.h, None, None, _p(ph), None, None))
+        return ph
 
     def bfs(self):
         i = self.info()

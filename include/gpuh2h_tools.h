@@ -47,6 +47,14 @@ int h2h_gen_uniform_pairs(int n_vertices, int64_t n, uint64_t seed, int *x, int 
  * uniform s over the loaded graph's arcs, so t lies within max_hops hops. */
 int h2h_gen_local_pairs(const h2h_graph *g, int64_t n, int max_hops, uint64_t seed, int *x, int *y);
 
+/* Measurement baseline, not a product path: the same batch answered with the
+ * reference's thread mapping (one thread per query, kernel_functions.cu:
+ * 1143-1296) on the same device index, so a bench can report the "plain GPU
+ * path" beside the tuned kernel.  Same arguments and results as
+ * h2h_query_batch. */
+int h2h_query_batch_plain(const h2h_graph *g, const int *x_dev, const int *y_dev, int *out_dev, int64_t n,
+                          int mode, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
