@@ -4,30 +4,36 @@
 // The reference runs one thread per partition cell and, for each elimination,
 // bubble-sorts the cell's remaining candidates by TDrank (degree + height,
 // degree, id), bubble-sorts the eliminated vertex's list, rewrites every
-// neighbour's list and scans lists linearly for fill-in.  The values it
-// produces depend only on:
+// neighbour's list and scans lists linearly for fill-in.  Its results depend
+// only on:
 //   * the candidate picked at each step: the minimum of the TDrank order, a
-//     strict total order because ids are unique -- so a block-wide argmin
-//     over keys kept in shared memory picks the same vertex;
-//   * the content of each list as a sequence: stable sorts by neighbour id
-//     (rank sort on (id << 32 | position) keys gives the same permutation),
-//     the duplicate merge carry (:339-351), the "recount" that leaves the
-//     size unchanged when no valid entry remains (:353-360, :381-388), and
-//     fill-in appends in the order the pair loop (:392-457) reaches them.
-// Here one CTA owns a cell.  Per elimination: argmin over the candidate keys
-// (shared memory), the eliminated vertex's list is staged and sorted in
-// shared memory, then each warp takes whole neighbour lists: delete the
-// back-edge, stable-sort, binary-search every other neighbour (first match =
-// lower_bound on the sorted prefix) and append misses in neighbour order.
-// Lists of different neighbours are disjoint, so warps never conflict.
-// Lists longer than a warp buffer are handled by the whole CTA afterwards.
+//     strict total order because ids are unique -- a block-wide argmin over
+//     keys kept in shared memory picks the same vertex;
+//   * each list as a sequence: stable sorts by neighbour id, the duplicate
+//     merge carry of the eliminated vertex's list (:339-351), the "recount"
+//     that leaves a size unchanged when no valid entry remains (:353-360,
+//     :381-388), first-match fill-in updates and appends (:392-457).
+// Every list is stable-sorted once up front and kept sorted: a stable sort
+// of the reference's [sorted run][appended run] is exactly the sorted merge
+// of the two runs, and every reader (next touch, own-list merge, the global
+// heap's first-seen emplace) sees the same sequence.  A list whose valid
+// entries all vanish keeps the reference's stale size as a prefix of junk
+// entries (`ljunk`), and later appends land after them, as in the reference.
 //
-// Degree/height keys follow :462-476: a neighbour's height becomes
-// max(height, HeightNow + 1) where HeightNow is the picked key's height, and
-// the first pick of a cell uses the stale keys (input degree, height 0)
-// written by makeAdjcentNode.
+// One CTA owns a cell.  Per elimination: argmin over the candidate keys, the
+// eliminated vertex's sorted list is staged in shared memory and merged,
+// then each warp takes whole neighbour lists and rebuilds them with a
+// merge-path union of (list minus v) and (the other neighbours), two linear
+// walks per lane after one co-rank search; a match updates the first entry of
+// that id (min weight), a miss inserts.  Warps never share a list.
+//
+// Keys follow :462-476: a neighbour's height becomes max(height, HeightNow+1)
+// with HeightNow the picked key's height; the first pick of a cell uses the
+// stale keys (input degree, height 0) written by makeAdjcentNode.
 #include <algorithm>
 #include <climits>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 
 #include "graph.h"
@@ -36,18 +42,18 @@ namespace gh {
 
 namespace {
 
-constexpr uint32_t kIdxMask = 0xffffffffu;
-constexpr int kErrOverflow = 1;  // a list outgrew its LUB capacity (reference corrupts memory)
-constexpr int kErrEmpty = 2;     // eliminated vertex without neighbours (reference reads ID_hash[INT_MAX])
-constexpr int kErrScratch = 3;   // a list outgrew the per-level staging bound
+constexpr int kErrOverflow = 1;  // a list outgrew its LUB capacity (the reference corrupts memory)
+constexpr int kErrEmpty = 2;     // eliminated a vertex without neighbours (the reference reads out of bounds)
+constexpr int kErrStaging = 3;   // a list outgrew the per-level staging bound
 
 struct LevelArgs {
   int *slot_nbr;
   int *slot_w;
   const int64_t *slot_off;
-  int *lsize;
+  int *lsize;             // list length, junk prefix included (CHTreeHash.first)
+  int *ljunk;             // leading stale entries of the list
   const int *cap;
-  int *height;
+  int *height;            // CHInfo.second
   int *elim;              // candidate ids per cell range; rewritten in elimination order
   const int *deg0;        // input degree (stale first-pick key)
   const int *cell_start;
@@ -56,64 +62,14 @@ struct LevelArgs {
   int *err;               // first error code (0 = none)
   int cell_lo;            // first cell index of the level
   int kmax;               // max candidates in a cell of this level
-  int lmax;               // max list length in a cell of this level
-  int wbuf;               // per-warp list buffer (entries)
+  int lmax;               // bound on valid list entries in a cell of this level
   int keys_in_smem;       // candidate keys in shared memory (else scratch)
-  int lists_in_smem;      // own-list + CTA sort buffers in shared memory (else scratch)
-  char *scratch;          // global staging slab, per CTA stride bytes
+  int lists_in_smem;      // list staging in shared memory (else scratch)
+  char *scratch;          // global staging slab, scratch_stride bytes per CTA
   int64_t scratch_stride;
 };
 
 __device__ __forceinline__ void set_err(int *err, int code) { atomicCAS(err, 0, code); }
-
-// Stable ascending sort of `key[0..s)` (distinct 64-bit keys) by a bitonic
-// network over the next power of two; comparators that reach past s are
-// skipped, which is the same as padding with +infinity.  `tid/nthr` span the
-// cooperating threads; SYNC is __syncwarp or __syncthreads.
-template <bool BLOCK>
-__device__ void bitonic_sort(uint64_t *key, int s, int tid, int nthr) {
-  if (s <= 1) return;
-  int P = 1;
-  while (P < s) P <<= 1;
-  const int half_p = P >> 1;
-  for (int k = 2; k <= P; k <<= 1) {
-    const int hk = k >> 1;
-    const int lg = __ffs(hk) - 1;
-    for (int t = tid; t < half_p; t += nthr) {
-      int lo = ((t >> lg) << (lg + 1)) + (t & (hk - 1));
-      int hi = lo ^ (k - 1);
-      if (hi < s) {
-        uint64_t a = key[lo], b = key[hi];
-        if (a > b) { key[lo] = b; key[hi] = a; }
-      }
-    }
-    if (BLOCK) __syncthreads(); else __syncwarp();
-    for (int m = k >> 2; m > 0; m >>= 1) {
-      const int lm = __ffs(m) - 1;
-      for (int t = tid; t < half_p; t += nthr) {
-        int lo = ((t >> lm) << (lm + 1)) + (t & (m - 1));
-        int hi = lo + m;
-        if (hi < s) {
-          uint64_t a = key[lo], b = key[hi];
-          if (a > b) { key[lo] = b; key[hi] = a; }
-        }
-      }
-      if (BLOCK) __syncthreads(); else __syncwarp();
-    }
-  }
-}
-
-__device__ __forceinline__ int key_id(uint64_t k) { return (int)(k >> 32); }
-
-// lower_bound of id x in sorted keys[0..n)
-__device__ __forceinline__ int lower_bound_id(const uint64_t *keys, int n, int x) {
-  int lo = 0, hi = n;
-  while (lo < hi) {
-    int mid = (lo + hi) >> 1;
-    if (key_id(keys[mid]) < x) lo = mid + 1; else hi = mid;
-  }
-  return lo;
-}
 
 struct Cand {
   int *id, *deg, *third;
@@ -125,100 +81,119 @@ __device__ __forceinline__ bool key_less(int s1, int d1, int i1, int s2, int d2,
   return i1 < i2;
 }
 
-// One neighbour list: delete v, stable sort, recount, fill-in against the
-// eliminated vertex's sorted list (anbr/aw, c entries, own index iu).
-// Runs on a warp (BLOCK=false) or on the whole CTA (BLOCK=true).
-template <bool BLOCK>
-__device__ void process_neighbour(const LevelArgs &A, int u, int wu, int iu, int v, int hnow, const int *anbr,
-                                  const int *aw, int c, uint64_t *key, int *worig, int tid, int nthr, Cand cand,
-                                  int *bcast) {
-  const int64_t off = A.slot_off[u];
-  const int s = A.lsize[u];
-  // load with the back-edge to v replaced by INT_MAX (kernel_functions.cu:364-375)
-  bool unsorted = false;
-  for (int i = tid; i < s; i += nthr) {
-    int nb = A.slot_nbr[off + i];
-    if (nb == v) nb = INT_MAX;
-    key[i] = ((uint64_t)(uint32_t)nb << 32) | (uint32_t)i;
-    worig[i] = A.slot_w[off + i];
+// Q = the eliminated vertex's list without entry iu.
+__device__ __forceinline__ int q_at(const int *a, int iu, int q) { return a[q < iu ? q : q + 1]; }
+
+// Merge-path co-rank: number of P entries among the first k outputs of the
+// stable merge of P and Q (ties take P first).
+__device__ __forceinline__ int corank(const int *pid, int np, const int *aid, int iu, int nq, int k) {
+  int lo = max(0, k - nq), hi = min(k, np);
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (pid[mid] <= q_at(aid, iu, k - 1 - mid)) lo = mid + 1; else hi = mid;
   }
-  if (BLOCK) __syncthreads(); else __syncwarp();
-  for (int i = tid; i + 1 < s; i += nthr)
-    if (key_id(key[i]) > key_id(key[i + 1])) unsorted = true;
-  if (BLOCK) unsorted = __syncthreads_or(unsorted);
-  else unsorted = __any_sync(0xffffffffu, unsorted);
-  if (unsorted) bitonic_sort<BLOCK>(key, s, tid, nthr);
-  // write the sorted list back; valid entries form the prefix after the sort
-  for (int i = tid; i < s; i += nthr) {
-    uint64_t k = key[i];
-    A.slot_nbr[off + i] = key_id(k);
-    A.slot_w[off + i] = worig[k & kIdxMask];
-  }
-  const int cu = lower_bound_id(key, s, INT_MAX);
-  const int size = cu > 0 ? cu : s;  // recount leaves the size unchanged when nothing valid remains
-  if (BLOCK) __syncthreads(); else __syncwarp();
-  // fill-in: every other neighbour x of v, in v's sorted order
-  int appended = 0;
-  for (int base = 0; base < c; base += nthr) {
-    int i = base + tid;
-    bool miss = false;
-    int x = 0, len = 0;
-    if (i < c && i != iu) {
-      x = anbr[i];
-      len = wu + aw[i];
-      int p = lower_bound_id(key, size, x);
-      if (p < size && key_id(key[p]) == x) {
-        if (A.slot_w[off + p] > len) A.slot_w[off + p] = len;
-      } else {
-        miss = true;
-      }
-    }
-    int rank, total;
-    if (BLOCK) {
-      // block-wide exclusive rank of misses
-      const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-      unsigned bal = __ballot_sync(0xffffffffu, miss);
-      if (lane == 0) bcast[wid] = __popc(bal);
-      __syncthreads();
-      int before = 0;
-      total = 0;
-      for (int w = 0; w < nw; w++) {
-        if (w < wid) before += bcast[w];
-        total += bcast[w];
-      }
-      rank = before + __popc(bal & ((1u << lane) - 1u));
-      __syncthreads();
-    } else {
-      unsigned bal = __ballot_sync(0xffffffffu, miss);
-      rank = __popc(bal & ((1u << tid) - 1u));
-      total = __popc(bal);
-    }
-    if (miss) {
-      int pos = size + appended + rank;
-      if (pos >= A.cap[u]) {
-        set_err(A.err, kErrOverflow);
-      } else {
-        A.slot_nbr[off + pos] = x;
-        A.slot_w[off + pos] = len;
-      }
-    }
-    appended += total;
-  }
-  if (tid == 0) {
-    int ns = size + appended;
-    A.lsize[u] = ns > A.cap[u] ? A.cap[u] : ns;
-    int h = A.height[u];
-    A.height[u] = (hnow + 1 > h) ? hnow + 1 : h;
-    int p = A.cpos[u];
-    if (p >= 0) {  // a remaining candidate of this cell: refresh its key
-      cand.deg[p] = A.lsize[u];
-      cand.third[p] = A.height[u];
-    }
-  }
-  if (BLOCK) __syncthreads(); else __syncwarp();
+  return lo;
 }
 
-__global__ void __launch_bounds__(256) contract_level_kernel(LevelArgs A) {
+// Rebuild neighbour u's list for the elimination of v (one warp):
+//   P = valid entries of u's list except v (kernel_functions.cu:364-390),
+//   output = P with the first entry of every matched id min-updated, plus the
+//   unmatched members of Q inserted in order (:392-457).
+__device__ void merge_neighbour(const LevelArgs &A, int u, int wu, int iu, int v, int hnow, const int *aid,
+                                const int *aw, int c, int *pid, int *pw, int lane, Cand cand) {
+  const int64_t off = A.slot_off[u];
+  const int s = A.lsize[u];
+  const int J = A.ljunk[u];
+  // stage P with v removed (stable compaction)
+  int np = 0;
+  for (int base = J; base < s; base += 32) {
+    const int idx = base + lane;
+    int x = INT_MAX, w = 0;
+    if (idx < s) { x = A.slot_nbr[off + idx]; w = A.slot_w[off + idx]; }
+    const bool keep = idx < s && x != v;
+    const unsigned bal = __ballot_sync(0xffffffffu, keep);
+    if (keep) {
+      const int pos = np + __popc(bal & ((1u << lane) - 1u));
+      pid[pos] = x;
+      pw[pos] = w;
+    }
+    np += __popc(bal);
+  }
+  __syncwarp();
+  const int nq = c - 1;
+  const int Jn = np > 0 ? 0 : s;  // nothing valid left: the reference keeps its stale size
+  const int total_len = np + nq;
+  const int seg = (total_len + 31) >> 5;
+  const int k0 = min(lane * seg, total_len), k1 = min(k0 + seg, total_len);
+  const int i0 = corank(pid, np, aid, iu, nq, k0);
+  // pass 1: count outputs, apply matched updates to the first entry of the id
+  int cnt = 0;
+  {
+    int i = i0, j = k0 - i0;
+    for (int t = k0; t < k1; t++) {
+      if (i < np && (j >= nq || pid[i] <= q_at(aid, iu, j))) {
+        i++;
+        cnt++;
+      } else {
+        const int x = q_at(aid, iu, j);
+        if (i > 0 && pid[i - 1] == x) {
+          int f = i - 1;
+          while (f > 0 && pid[f - 1] == x) f--;
+          atomicMin(pw + f, wu + q_at(aw, iu, j));
+        } else {
+          cnt++;
+        }
+        j++;
+      }
+    }
+  }
+  __syncwarp();
+  int incl = cnt;
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += y;
+  }
+  const int total = __shfl_sync(0xffffffffu, incl, 31);
+  const bool fits = Jn + total <= A.cap[u];
+  if (fits) {
+    int o = incl - cnt;
+    int i = i0, j = k0 - i0;
+    for (int t = k0; t < k1; t++) {
+      if (i < np && (j >= nq || pid[i] <= q_at(aid, iu, j))) {
+        A.slot_nbr[off + Jn + o] = pid[i];
+        A.slot_w[off + Jn + o] = pw[i];
+        o++;
+        i++;
+      } else {
+        const int x = q_at(aid, iu, j);
+        if (!(i > 0 && pid[i - 1] == x)) {
+          A.slot_nbr[off + Jn + o] = x;
+          A.slot_w[off + Jn + o] = wu + q_at(aw, iu, j);
+          o++;
+        }
+        j++;
+      }
+    }
+    for (int k = lane; k < Jn; k += 32) A.slot_nbr[off + k] = INT_MAX;
+  }
+  if (lane == 0) {
+    if (!fits) set_err(A.err, kErrOverflow);
+    const int ns = fits ? Jn + total : s;
+    A.lsize[u] = ns;
+    A.ljunk[u] = fits ? Jn : J;
+    const int h = A.height[u];
+    const int hn = (hnow + 1 > h) ? hnow + 1 : h;
+    A.height[u] = hn;
+    const int p = A.cpos[u];
+    if (p >= 0) {  // a remaining candidate of this cell: refresh its key
+      cand.deg[p] = ns;
+      cand.third[p] = hn;
+    }
+  }
+  __syncwarp();
+}
+
+__global__ void __launch_bounds__(512) contract_level_kernel(LevelArgs A) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int cell = A.cell_lo + blockIdx.x;
   const int start = A.cell_start[cell];
@@ -227,7 +202,6 @@ __global__ void __launch_bounds__(256) contract_level_kernel(LevelArgs A) {
   const int tid = threadIdx.x, nthr = blockDim.x;
   const int lane = tid & 31, wid = tid >> 5, nw = nthr >> 5;
 
-  // ---- carve staging areas (shared memory, or this CTA's scratch slab)
   unsigned char *sp = smem;
   unsigned char *gp = (unsigned char *)A.scratch + (int64_t)blockIdx.x * A.scratch_stride;
   auto take = [&](bool in_smem, int64_t bytes) -> void * {
@@ -236,23 +210,19 @@ __global__ void __launch_bounds__(256) contract_level_kernel(LevelArgs A) {
     if (in_smem) { r = sp; sp += bytes; } else { r = gp; gp += bytes; }
     return r;
   };
-  __shared__ int bcast[32];
   __shared__ int s_red_sum[32], s_red_deg[32], s_red_id[32], s_red_pos[32];
-  __shared__ int s_v, s_hnow, s_c, s_stop, s_nbig;
+  __shared__ int s_v, s_hnow, s_c, s_stop;
   Cand cand;
   cand.id = (int *)take(A.keys_in_smem, sizeof(int) * A.kmax);
   cand.deg = (int *)take(A.keys_in_smem, sizeof(int) * A.kmax);
   cand.third = (int *)take(A.keys_in_smem, sizeof(int) * A.kmax);
-  int *anbr = (int *)take(A.lists_in_smem, sizeof(int) * A.lmax);
+  int *aid = (int *)take(A.lists_in_smem, sizeof(int) * A.lmax);
   int *aw = (int *)take(A.lists_in_smem, sizeof(int) * A.lmax);
-  uint64_t *bkey = (uint64_t *)take(A.lists_in_smem, sizeof(uint64_t) * A.lmax);
-  int *bw = (int *)take(A.lists_in_smem, sizeof(int) * A.lmax);
-  int *big = (int *)take(A.lists_in_smem, sizeof(int) * A.lmax);  // deferred neighbour indices
-  uint64_t *wkey = (uint64_t *)take(true, sizeof(uint64_t) * A.wbuf * nw) + (int64_t)wid * A.wbuf;
-  int *ww = (int *)take(true, sizeof(int) * A.wbuf * nw) + (int64_t)wid * A.wbuf;
+  int *pid = (int *)take(A.lists_in_smem, sizeof(int) * A.lmax * nw) + (int64_t)wid * A.lmax;
+  int *pw = (int *)take(A.lists_in_smem, sizeof(int) * A.lmax * nw) + (int64_t)wid * A.lmax;
 
   for (int i = tid; i < k; i += nthr) {
-    int v = A.elim[start + i];
+    const int v = A.elim[start + i];
     cand.id[i] = v;
     cand.deg[i] = A.deg0[v];
     cand.third[i] = 0;
@@ -265,12 +235,12 @@ __global__ void __launch_bounds__(256) contract_level_kernel(LevelArgs A) {
     // ---- 1. argmin of (deg + height, deg, id) over candidates [j, k)
     int bs = INT_MAX, bd = INT_MAX, bi = INT_MAX, bp = -1;
     for (int i = j + tid; i < k; i += nthr) {
-      int d = cand.deg[i], t = cand.third[i], id = cand.id[i];
+      const int d = cand.deg[i], t = cand.third[i], id = cand.id[i];
       if (bp < 0 || key_less(d + t, d, id, bs, bd, bi)) { bs = d + t; bd = d; bi = id; bp = i; }
     }
     for (int o = 16; o > 0; o >>= 1) {
-      int os = __shfl_down_sync(0xffffffffu, bs, o), od = __shfl_down_sync(0xffffffffu, bd, o);
-      int oi = __shfl_down_sync(0xffffffffu, bi, o), op = __shfl_down_sync(0xffffffffu, bp, o);
+      const int os = __shfl_down_sync(0xffffffffu, bs, o), od = __shfl_down_sync(0xffffffffu, bd, o);
+      const int oi = __shfl_down_sync(0xffffffffu, bi, o), op = __shfl_down_sync(0xffffffffu, bp, o);
       if (op >= 0 && (bp < 0 || key_less(os, od, oi, bs, bd, bi))) { bs = os; bd = od; bi = oi; bp = op; }
     }
     if (lane == 0) { s_red_sum[wid] = bs; s_red_deg[wid] = bd; s_red_id[wid] = bi; s_red_pos[wid] = bp; }
@@ -283,10 +253,10 @@ __global__ void __launch_bounds__(256) contract_level_kernel(LevelArgs A) {
         }
       }
       // ---- 2. move the pick to position j
-      int v = cand.id[rp];
-      int hn = cand.third[rp];
+      const int v = cand.id[rp];
+      const int hn = cand.third[rp];
       if (rp != j) {
-        int u = cand.id[j];
+        const int u = cand.id[j];
         cand.id[rp] = u; cand.deg[rp] = cand.deg[j]; cand.third[rp] = cand.third[j];
         A.cpos[u] = rp;
         cand.id[j] = v; cand.deg[j] = rd; cand.third[j] = hn;
@@ -298,78 +268,56 @@ __global__ void __launch_bounds__(256) contract_level_kernel(LevelArgs A) {
     }
     __syncthreads();
     const int v = s_v, hnow = s_hnow;
-    // ---- 3. own list: stable sort, merge duplicates, compact (kernel_functions.cu:338-361)
+    // ---- 3. own list: valid part is sorted; merge duplicates, drop junk (:338-361)
     const int64_t voff = A.slot_off[v];
-    const int sv = A.lsize[v];
-    if (sv > A.lmax) { if (tid == 0) { set_err(A.err, kErrScratch); s_stop = 1; } }
+    const int vJ = A.ljunk[v];
+    const int sv = A.lsize[v] - vJ;
+    if (sv > A.lmax) { if (tid == 0) { set_err(A.err, kErrStaging); s_stop = 1; } }
     __syncthreads();
     if (s_stop) return;
     for (int i = tid; i < sv; i += nthr) {
-      bkey[i] = ((uint64_t)(uint32_t)A.slot_nbr[voff + i] << 32) | (uint32_t)i;
-      bw[i] = A.slot_w[voff + i];
+      aid[i] = A.slot_nbr[voff + vJ + i];
+      aw[i] = A.slot_w[voff + vJ + i];
     }
     __syncthreads();
-    bitonic_sort<true>(bkey, sv, tid, nthr);
     bool dup = false;
-    for (int i = tid; i < sv; i += nthr) {
-      anbr[i] = key_id(bkey[i]);
-      aw[i] = bw[bkey[i] & kIdxMask];
-    }
-    __syncthreads();
     for (int i = tid + 1; i < sv; i += nthr)
-      if (anbr[i] == anbr[i - 1] && anbr[i] != INT_MAX) dup = true;
+      if (aid[i] == aid[i - 1]) dup = true;
     dup = __syncthreads_or(dup);
-    if (dup && tid == 0) {
-      // carry merge then stable compaction (the second stable sort only moves the INT_MAX entries)
-      for (int i = 1; i < sv; i++) {
-        if (anbr[i] == anbr[i - 1] && anbr[i] != INT_MAX) {
-          if (aw[i - 1] < aw[i]) aw[i] = aw[i - 1];
-          anbr[i - 1] = INT_MAX;
-        }
-      }
-      int c = 0;
-      for (int i = 0; i < sv; i++) if (anbr[i] != INT_MAX) { anbr[c] = anbr[i]; aw[c] = aw[i]; c++; }
-      for (int i = c; i < sv; i++) anbr[i] = INT_MAX;
-    }
-    __syncthreads();
     if (tid == 0) {
-      int c = 0;
-      while (c < sv && anbr[c] != INT_MAX) c++;  // valid entries form the prefix
+      int c = sv;
+      if (dup) {  // carry merge (the later entry keeps the smaller weight), then compaction
+        for (int i = 1; i < sv; i++) {
+          if (aid[i] == aid[i - 1] && aid[i] != INT_MAX) {
+            if (aw[i - 1] < aw[i]) aw[i] = aw[i - 1];
+            aid[i - 1] = INT_MAX;
+          }
+        }
+        c = 0;
+        for (int i = 0; i < sv; i++) if (aid[i] != INT_MAX) { aid[c] = aid[i]; aw[c] = aw[i]; c++; }
+      }
       s_c = c;
       if (c == 0) { set_err(A.err, kErrEmpty); s_stop = 1; }
-      else A.lsize[v] = c;
-      s_nbig = 0;
+      else { A.lsize[v] = c; A.ljunk[v] = 0; }
     }
     __syncthreads();
     if (s_stop) return;
     const int c = s_c;
-    for (int i = tid; i < c; i += nthr) { A.slot_nbr[voff + i] = anbr[i]; A.slot_w[voff + i] = aw[i]; }
-    // ---- 4. neighbours, one warp each; long lists deferred to the CTA
+    for (int i = tid; i < c; i += nthr) { A.slot_nbr[voff + i] = aid[i]; A.slot_w[voff + i] = aw[i]; }
+    // ---- 4. neighbours, one warp each
     for (int i = wid; i < c; i += nw) {
-      const int u = anbr[i];
-      const int su = A.lsize[u];
-      if (su > A.wbuf) {
-        if (lane == 0) big[atomicAdd(&s_nbig, 1)] = i;
+      const int u = aid[i];
+      if (A.lsize[u] - A.ljunk[u] > A.lmax) {
+        if (lane == 0) set_err(A.err, kErrStaging);
         continue;
       }
-      process_neighbour<false>(A, u, aw[i], i, v, hnow, anbr, aw, c, wkey, ww, lane, 32, cand, nullptr);
+      merge_neighbour(A, u, aw[i], i, v, hnow, aid, aw, c, pid, pw, lane, cand);
     }
     __syncthreads();
-    const int nbig = s_nbig;
-    for (int b = 0; b < nbig; b++) {
-      const int i = big[b];
-      const int u = anbr[i];
-      if (A.lsize[u] > A.lmax) {
-        if (tid == 0) { set_err(A.err, kErrScratch); s_stop = 1; }
-        __syncthreads();
-        return;
-      }
-      process_neighbour<true>(A, u, aw[i], i, v, hnow, anbr, aw, c, bkey, bw, tid, nthr, cand, bcast);
-    }
     // ---- 5. after the first pick every remaining key becomes live (:471-475)
     if (j == 0) {
       for (int i = 1 + tid; i < k; i += nthr) {
-        int u = cand.id[i];
+        const int u = cand.id[i];
         cand.deg[i] = A.lsize[u];
         cand.third[i] = A.height[u];
       }
@@ -380,11 +328,20 @@ __global__ void __launch_bounds__(256) contract_level_kernel(LevelArgs A) {
 
 __global__ void scatter_adjacency_kernel(const int *adj_off, const int *adj_v, const int *adj_w,
                                          const int64_t *slot_off, int *slot_nbr, int *slot_w, int n) {
+  // input lists in file order, stable-sorted by neighbour id (insertion sort)
   for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
-    int64_t o = slot_off[v];
-    for (int e = adj_off[v]; e < adj_off[v + 1]; e++) {
-      slot_nbr[o + (e - adj_off[v])] = adj_v[e];
-      slot_w[o + (e - adj_off[v])] = adj_w[e];
+    const int64_t o = slot_off[v];
+    const int b = adj_off[v], e = adj_off[v + 1];
+    for (int i = b; i < e; i++) {
+      const int x = adj_v[i], w = adj_w[i];
+      int k = i - b;
+      while (k > 0 && slot_nbr[o + k - 1] > x) {
+        slot_nbr[o + k] = slot_nbr[o + k - 1];
+        slot_w[o + k] = slot_w[o + k - 1];
+        k--;
+      }
+      slot_nbr[o + k] = x;
+      slot_w[o + k] = w;
     }
   }
 }
@@ -395,8 +352,8 @@ __global__ void gather_lists_kernel(const int64_t *slot_off, const int *lsize, c
   const int lane = threadIdx.x & 31;
   for (int64_t v = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; v < n;
        v += (gridDim.x * (int64_t)blockDim.x) >> 5) {
-    int64_t so = slot_off[v], oo = out_off[v];
-    int s = lsize[v];
+    const int64_t so = slot_off[v], oo = out_off[v];
+    const int s = lsize[v];
     for (int i = lane; i < s; i += 32) {
       out_nbr[oo + i] = slot_nbr[so + i];
       out_w[oo + i] = slot_w[so + i];
@@ -445,14 +402,14 @@ void contract_partition_levels_gpu(Graph &g, std::vector<int64_t> &lst_off, std:
   int *d_slot_nbr = dalloc<int>(g.lub), *d_slot_w = dalloc<int>(g.lub);
   int64_t *d_slot_off = dalloc<int64_t>(n);
   int *d_lsize = dalloc<int>(n), *d_cap = dalloc<int>(n), *d_height = dalloc<int>(n), *d_elim = dalloc<int>(n);
-  int *d_deg0 = dalloc<int>(n), *d_cpos = dalloc<int>(n), *d_err = dalloc<int>(1);
+  int *d_deg0 = dalloc<int>(n), *d_cpos = dalloc<int>(n), *d_err = dalloc<int>(1), *d_ljunk = dalloc<int>(n);
   int *d_cell_start = dalloc<int>(g.cell_start.size()), *d_cell_count = dalloc<int>(g.cell_count.size());
   int *d_adj_off = dalloc<int>(n + 1), *d_adj_v = dalloc<int>(g.m), *d_adj_w = dalloc<int>(g.m);
   char *d_scratch = nullptr;
   int64_t scratch_bytes = 0;
   auto cleanup = [&]() {
     cudaFree(d_slot_nbr); cudaFree(d_slot_w); cudaFree(d_slot_off); cudaFree(d_lsize); cudaFree(d_cap);
-    cudaFree(d_height); cudaFree(d_elim); cudaFree(d_deg0); cudaFree(d_cpos); cudaFree(d_err);
+    cudaFree(d_height); cudaFree(d_elim); cudaFree(d_deg0); cudaFree(d_cpos); cudaFree(d_err); cudaFree(d_ljunk);
     cudaFree(d_cell_start); cudaFree(d_cell_count); cudaFree(d_adj_off); cudaFree(d_adj_v); cudaFree(d_adj_w);
     if (d_scratch) cudaFree(d_scratch);
   };
@@ -464,6 +421,7 @@ void contract_partition_levels_gpu(Graph &g, std::vector<int64_t> &lst_off, std:
     GH_CUDA(cudaMemcpy(d_deg0, deg.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
     GH_CUDA(cudaMemcpy(d_cap, g.cap.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
     GH_CUDA(cudaMemcpy(d_height, zeros.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
+    GH_CUDA(cudaMemcpy(d_ljunk, zeros.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
     GH_CUDA(cudaMemcpy(d_cpos, minus1.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
     GH_CUDA(cudaMemcpy(d_elim, g.elim.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
     GH_CUDA(cudaMemcpy(d_cell_start, g.cell_start.data(), sizeof(int) * g.cell_start.size(), cudaMemcpyHostToDevice));
@@ -482,7 +440,10 @@ void contract_partition_levels_gpu(Graph &g, std::vector<int64_t> &lst_off, std:
     clk.reset();
 
     const int smem_dyn = enable_max_dynamic_smem(contract_level_kernel);
-    const int kThreads = 256, kWarps = kThreads / 32;
+    const bool trace = std::getenv("GPUH2H_TRACE") != nullptr;
+    int nsm = 0, dev = 0;
+    GH_CUDA(cudaGetDevice(&dev));
+    GH_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
     for (int h = g.H; h > g.C; h--) {
       const int64_t lo = (int64_t(1) << (h - 1)) - 1, hi = (int64_t(1) << h) - 2;
       const int ncell = (int)(hi - lo + 1);
@@ -509,20 +470,20 @@ void contract_partition_levels_gpu(Graph &g, std::vector<int64_t> &lst_off, std:
       A.slot_nbr = d_slot_nbr; A.slot_w = d_slot_w; A.slot_off = d_slot_off; A.lsize = d_lsize; A.cap = d_cap;
       A.height = d_height; A.elim = d_elim; A.deg0 = d_deg0; A.cell_start = d_cell_start;
       A.cell_count = d_cell_count; A.cpos = d_cpos; A.err = d_err; A.cell_lo = (int)lo;
-      A.kmax = kmax; A.lmax = lmax;
-      A.wbuf = std::min(lmax, 256);
+      A.kmax = kmax; A.lmax = lmax; A.ljunk = d_ljunk;
       auto al = [](int64_t b) { return (b + 15) & ~int64_t(15); };
-      int64_t keys_b = 3 * al(sizeof(int) * (int64_t)kmax);
-      int64_t lists_b = al(4LL * lmax) * 2 + al(8LL * lmax) + al(4LL * lmax) * 2;
-      int64_t warp_b = al(8LL * A.wbuf * kWarps) + al(4LL * A.wbuf * kWarps);
+      const int64_t keys_b = 3 * al(sizeof(int) * (int64_t)kmax);
+      auto lists_bytes = [&](int nw) { return 2 * al(4LL * lmax) + 2 * al(4LL * lmax * nw); };
       const int64_t budget = smem_dyn;
+      // few cells (top levels): 16 warps per cell; many cells: 8 warps, several CTAs per SM
+      int nw = ncell < nsm ? 16 : 8;
+      while (nw > 4 && keys_b + lists_bytes(nw) > budget) nw >>= 1;
       A.keys_in_smem = 1;
       A.lists_in_smem = 1;
-      int64_t smem = keys_b + lists_b + warp_b;
-      if (smem > budget) { A.lists_in_smem = 0; smem = keys_b + warp_b; }
-      if (smem > budget) { A.keys_in_smem = 0; smem = warp_b; }
-      GH_CHECK(smem <= budget, H2H_ERR_DEVICE, "contraction staging does not fit shared memory");
-      int64_t stride = (A.keys_in_smem ? 0 : keys_b) + (A.lists_in_smem ? 0 : lists_b);
+      int64_t smem = keys_b + lists_bytes(nw);
+      if (smem > budget) { A.lists_in_smem = 0; smem = keys_b; }
+      if (smem > budget) { A.keys_in_smem = 0; smem = 0; }
+      int64_t stride = (A.keys_in_smem ? 0 : keys_b) + (A.lists_in_smem ? 0 : lists_bytes(nw));
       stride = al(stride);
       if (stride * ncell > scratch_bytes) {
         if (d_scratch) cudaFree(d_scratch);
@@ -532,15 +493,28 @@ void contract_partition_levels_gpu(Graph &g, std::vector<int64_t> &lst_off, std:
       }
       A.scratch = d_scratch;
       A.scratch_stride = stride;
-      contract_level_kernel<<<ncell, kThreads, (size_t)smem>>>(A);
+      cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+      if (trace) { cudaEventCreate(&ev0); cudaEventCreate(&ev1); cudaEventRecord(ev0); }
+      contract_level_kernel<<<ncell, nw * 32, (size_t)smem>>>(A);
       GH_CUDA(cudaGetLastError());
+      if (trace) {
+        cudaEventRecord(ev1);
+        cudaEventSynchronize(ev1);
+        float ms = 0;
+        cudaEventElapsedTime(&ms, ev0, ev1);
+        std::fprintf(stderr, "[gpuh2h] contract level %d: %d cells x %d warps, kmax %d, lmax %d, smem %lld (keys %s, lists %s): %.3f ms\n",
+                     h, ncell, nw, kmax, lmax, (long long)smem, A.keys_in_smem ? "smem" : "global",
+                     A.lists_in_smem ? "smem" : "global", ms);
+        cudaEventDestroy(ev0);
+        cudaEventDestroy(ev1);
+      }
     }
     GH_CUDA(cudaDeviceSynchronize());
     int err = 0;
     GH_CUDA(cudaMemcpy(&err, d_err, sizeof(int), cudaMemcpyDeviceToHost));
     GH_CHECK(err == 0, H2H_ERR_DEVICE,
              err == kErrOverflow ? "contraction: a list outgrew its LUB capacity"
-             : err == kErrEmpty  ? "contraction: eliminated a vertex with an empty list (disconnected input)"
+             : err == kErrEmpty ? "contraction: eliminated a vertex with an empty list (disconnected input)"
                                  : "contraction: list outgrew the staging bound");
     g.t.td_gpu = clk.us();
     clk.reset();

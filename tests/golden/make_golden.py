@@ -113,6 +113,18 @@ def main():
                     g0[tag + "/sha256/" + k] = np.frombuffer(bytes.fromhex(digest(ref[k])), np.uint8)
                     g0[tag + "/len/" + k] = np.array([len(ref[k])], np.int64)
                 g0[tag + "/dis_sample"] = ref["dis"][::97]
+        # the same grid with parallel arcs (tests/conftest.py:write_multigraph)
+        sys.path.insert(0, os.path.join(REPO, "tests"))
+        from conftest import write_multigraph
+        mfiles = write_multigraph(root)
+        for C in (1, 2):
+            ref = O.run_reference(*mfiles, CFG0["H"], C, 4, l4=True, pairs=pairs)
+            compare(ref, oracle_arrays(*mfiles, CFG0["H"], C, True, pairs), "multi/C%d" % C)
+            tag = "multi_C%d_L4" % C
+            for k in ("order", "father", "q_lca", "q_nolca"):
+                g0[tag + "/" + k] = ref[k]
+            for k in ("dis", "adj_id", "adj_w", "rmq_id", "pos_pos"):
+                g0[tag + "/sha256/" + k] = np.frombuffer(bytes.fromhex(digest(ref[k])), np.uint8)
     np.savez_compressed(os.path.join(HERE, "cfg0.npz"), **g0)
     print("wrote", os.path.join(HERE, "sample13.npz"), os.path.join(HERE, "cfg0.npz"))
 

@@ -89,3 +89,16 @@ def test_l3_lca_query_is_inexact_but_nolca_exact(golden0):
     l4 = golden0["cfg0_C1_L4/q_lca"]
     assert (l3 != l4).any()
     assert np.array_equal(golden0["cfg0_C1_L3/q_nolca"], l4)
+
+
+@pytest.mark.parametrize("C", [1, 2])
+def test_multigraph(multi_files, golden0, C):
+    tag = "multi_C%d_L4/" % C
+    pairs = golden0["pairs"]
+    g = O.OracleGraph(*multi_files, 6, C, 4).contract().build_labels(l4=True)
+    assert np.array_equal(g.order(), golden0[tag + "order"])
+    assert np.array_equal(g.father(), golden0[tag + "father"])
+    assert np.array_equal(_sha(g.labels()["dis"]), golden0[tag + "sha256/dis"])
+    ah, aid, aw = g.adj()
+    assert np.array_equal(_sha(aw), golden0[tag + "sha256/adj_w"])
+    assert np.array_equal(g.query_batch(pairs[:, 0], pairs[:, 1]), golden0[tag + "q_lca"])

@@ -80,6 +80,22 @@ def test_cfg0(cfg0_root, golden0, C, l4, pf):
     assert g.info()["gpu_vertices"] == golden0[tag + "gpu_vertices"][0]
 
 
+@pytest.mark.parametrize("C", [1, 2])
+def test_multigraph(multi_files, golden0, C):
+    """Parallel arcs: duplicate merge at elimination and first-match fill-in."""
+    import gpuh2h
+    tag = "multi_C%d_L4/" % C
+    g = build(multi_files, 6, C)
+    assert np.array_equal(g.order(), golden0[tag + "order"])
+    assert np.array_equal(g.tree()[0], golden0[tag + "father"])
+    ah, aid, aw = g.adj()
+    assert np.array_equal(_sha(aid), golden0[tag + "sha256/adj_id"])
+    assert np.array_equal(_sha(aw), golden0[tag + "sha256/adj_w"])
+    assert np.array_equal(_sha(g.labels()["dis"]), golden0[tag + "sha256/dis"])
+    pairs = golden0["pairs"]
+    assert np.array_equal(g.query(pairs[:, 0], pairs[:, 1], gpuh2h.QUERY_LCA), golden0[tag + "q_lca"])
+
+
 def test_query_edge_cases(cfg0_root, golden0):
     import gpuh2h
     g = build(gpuh2h.files_for(cfg0_root, "cfg0"), 6, 1)
