@@ -156,18 +156,7 @@ int h2h_contract(h2h_graph *h, int use_gpu_contract) {
              "GPU hot path");
     g.contract_device = use_gpu_contract;
     gh::build_elimination_sets(g);
-    std::vector<int64_t> off;
-    std::vector<int> nbr, w;
-    if (g.H != g.C) {
-      gh::contract_partition_levels_gpu(g, off, nbr, w);
-    } else {  // main.cu:96: no partition level runs on the GPU
-      off.assign(g.n + 1, 0);
-      for (int v = 0; v < g.n; v++) off[v + 1] = g.adj_off[v + 1];
-      nbr = g.adj_v;
-      w = g.adj_w;
-      g.height.assign(g.n, 0);
-    }
-    gh::contract_global_heap(g, off, nbr, w);
+    gh::contract_gpu(g);  // with H == C no partition level runs (main.cu:96): the heap takes every vertex
     gh::build_tree_and_rmq(g);
     g.contracted = true;
   });

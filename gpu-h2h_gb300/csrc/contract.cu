@@ -1,35 +1,47 @@
-// contract.cu -- partition-level vertex elimination on the GPU, the work of
-// makeCHPerHeight_2 / makeCHPerHeight_D_2 (kernel_functions.cu:309-553).
+// contract.cu -- vertex elimination on the GPU: the partition levels of
+// makeCHPerHeight_2 / makeCHPerHeight_D_2 (kernel_functions.cu:309-553) and
+// the global minimum-degree heap of TDInCPU / uploadCHset / CHUsingHeap_2
+// (Traditional_H2H.cu:6-118, :216-351), both as one elimination kernel.
 //
 // The reference runs one thread per partition cell and, for each elimination,
 // bubble-sorts the cell's remaining candidates by TDrank (degree + height,
 // degree, id), bubble-sorts the eliminated vertex's list, rewrites every
-// neighbour's list and scans lists linearly for fill-in.  Its results depend
+// neighbour's list and scans lists linearly for fill-in; the top levels go to
+// a std::set heap with hash-map adjacency on the host.  Its results depend
 // only on:
-//   * the candidate picked at each step: the minimum of the TDrank order, a
-//     strict total order because ids are unique -- a block-wide argmin over
-//     keys kept in shared memory picks the same vertex;
+//   * the vertex picked at each step: the minimum of the (degree + height,
+//     degree, id) order, a strict total order because ids are unique -- a
+//     block argmin over keys held in shared memory picks the same vertex;
 //   * each list as a sequence: stable sorts by neighbour id, the duplicate
 //     merge carry of the eliminated vertex's list (:339-351), the "recount"
 //     that leaves a size unchanged when no valid entry remains (:353-360,
 //     :381-388), first-match fill-in updates and appends (:392-457).
-// Every list is stable-sorted once up front and kept sorted: a stable sort
-// of the reference's [sorted run][appended run] is exactly the sorted merge
-// of the two runs, and every reader (next touch, own-list merge, the global
-// heap's first-seen emplace) sees the same sequence.  A list whose valid
-// entries all vanish keeps the reference's stale size as a prefix of junk
-// entries (`ljunk`), and later appends land after them, as in the reference.
+// Every list is stable-sorted once up front and kept sorted: a stable sort of
+// the reference's [sorted run][appended run] is exactly the sorted merge of
+// the two runs, and every reader (next touch, own-list merge, the heap's
+// first-seen emplace) sees the same sequence.  A list whose valid entries
+// all vanish keeps the reference's stale size as a prefix of junk entries
+// (`ljunk`); later appends land after them, as in the reference.
 //
-// One CTA owns a cell.  Per elimination: argmin over the candidate keys, the
-// eliminated vertex's sorted list is staged in shared memory and merged,
-// then each warp takes whole neighbour lists and rebuilds them with a
-// merge-path union of (list minus v) and (the other neighbours), two linear
-// walks per lane after one co-rank search; a match updates the first entry of
-// that id (min weight), a miss inserts.  Warps never share a list.
+// One thread-block cluster owns a cell (one CTA for the many small cells at
+// the bottom, up to 16 CTAs for the few large cells near the top).  Per
+// elimination the leader CTA takes the argmin and merges the eliminated
+// vertex's own list in shared memory; after a cluster barrier every warp of
+// every CTA rebuilds whole neighbour lists with a merge-path union of
+// (list minus v) and (the other neighbours) -- one co-rank search and two
+// linear walks per lane; a match min-updates the first entry of that id, a
+// miss inserts -- and writes candidate keys back into the leader's shared
+// memory.  Warps never share a list.
 //
-// Keys follow :462-476: a neighbour's height becomes max(height, HeightNow+1)
-// with HeightNow the picked key's height; the first pick of a cell uses the
-// stale keys (input degree, height 0) written by makeAdjcentNode.
+// Keys follow kernel_functions.cu:462-476: a neighbour's height becomes
+// max(height, HeightNow + 1) with HeightNow the picked key's height; the
+// first pick of a cell uses the stale keys (input degree, height 0) written
+// by makeAdjcentNode, after which every key is live.  The global heap is the
+// same loop over one "cell" holding every vertex of levels <= C, with live
+// keys from the start (valid-entry count, height) and first-seen duplicate
+// removal on entry (unordered_map::emplace), and empty lists stay empty.
+#include <cooperative_groups.h>
+
 #include <algorithm>
 #include <climits>
 #include <cstdio>
@@ -37,6 +49,8 @@
 #include <cstring>
 
 #include "graph.h"
+
+namespace cg = cooperative_groups;
 
 namespace gh {
 
@@ -46,27 +60,27 @@ constexpr int kErrOverflow = 1;  // a list outgrew its LUB capacity (the referen
 constexpr int kErrEmpty = 2;     // eliminated a vertex without neighbours (the reference reads out of bounds)
 constexpr int kErrStaging = 3;   // a list outgrew the per-level staging bound
 
-struct LevelArgs {
+struct ElimArgs {
   int *slot_nbr;
   int *slot_w;
-  const int64_t *slot_off;
+  int64_t *slot_off;      // list start (a heap list that outgrows its range moves)
   int *lsize;             // list length, junk prefix included (CHTreeHash.first)
   int *ljunk;             // leading stale entries of the list
-  const int *cap;
+  int *cap;               // list capacity
+  unsigned long long *pool_next;  // bump allocator over the slot arrays (heap mode)
+  int64_t pool_size;
   int *height;            // CHInfo.second
   int *elim;              // candidate ids per cell range; rewritten in elimination order
-  const int *deg0;        // input degree (stale first-pick key)
+  const int *key_deg0;    // first-pick degree key per vertex
+  const int *key_h0;      // first-pick height key per vertex (nullptr = 0)
   const int *cell_start;
   const int *cell_count;
-  int *cpos;              // vertex -> local candidate index while it is a candidate, else -1
+  int *cpos;              // vertex -> candidate index while it is a candidate of its cell, else -1
   int *err;               // first error code (0 = none)
-  int cell_lo;            // first cell index of the level
-  int kmax;               // max candidates in a cell of this level
-  int lmax;               // bound on valid list entries in a cell of this level
-  int keys_in_smem;       // candidate keys in shared memory (else scratch)
-  int lists_in_smem;      // list staging in shared memory (else scratch)
-  char *scratch;          // global staging slab, scratch_stride bytes per CTA
-  int64_t scratch_stride;
+  int cell_lo;            // first cell index of the launch
+  int kmax;               // max candidates in a cell of this launch
+  int lmax;               // bound on valid list entries in a cell of this launch
+  int heap_mode;          // 1: global heap semantics (live keys, no refresh, no junk)
 };
 
 __device__ __forceinline__ void set_err(int *err, int code) { atomicCAS(err, 0, code); }
@@ -99,17 +113,18 @@ __device__ __forceinline__ int corank(const int *pid, int np, const int *aid, in
 //   P = valid entries of u's list except v (kernel_functions.cu:364-390),
 //   output = P with the first entry of every matched id min-updated, plus the
 //   unmatched members of Q inserted in order (:392-457).
-__device__ void merge_neighbour(const LevelArgs &A, int u, int wu, int iu, int v, int hnow, const int *aid,
+// Mutable global data is read through L2 (ld.global.cg): other CTAs of the
+// cluster write it between cluster barriers.
+__device__ void merge_neighbour(const ElimArgs &A, int u, int wu, int iu, int v, int hnow, const int *aid,
                                 const int *aw, int c, int *pid, int *pw, int lane, Cand cand) {
-  const int64_t off = A.slot_off[u];
-  const int s = A.lsize[u];
-  const int J = A.ljunk[u];
-  // stage P with v removed (stable compaction)
+  int64_t off = __ldcg(A.slot_off + u);
+  const int s = __ldcg(A.lsize + u);
+  const int J = __ldcg(A.ljunk + u);
   int np = 0;
   for (int base = J; base < s; base += 32) {
     const int idx = base + lane;
     int x = INT_MAX, w = 0;
-    if (idx < s) { x = A.slot_nbr[off + idx]; w = A.slot_w[off + idx]; }
+    if (idx < s) { x = __ldcg(A.slot_nbr + off + idx); w = __ldcg(A.slot_w + off + idx); }
     const bool keep = idx < s && x != v;
     const unsigned bal = __ballot_sync(0xffffffffu, keep);
     if (keep) {
@@ -121,7 +136,8 @@ __device__ void merge_neighbour(const LevelArgs &A, int u, int wu, int iu, int v
   }
   __syncwarp();
   const int nq = c - 1;
-  const int Jn = np > 0 ? 0 : s;  // nothing valid left: the reference keeps its stale size
+  // nothing valid left: the partition kernel keeps its stale size, a heap map is empty
+  const int Jn = (np > 0 || A.heap_mode) ? 0 : s;
   const int total_len = np + nq;
   const int seg = (total_len + 31) >> 5;
   const int k0 = min(lane * seg, total_len), k1 = min(k0 + seg, total_len);
@@ -154,7 +170,26 @@ __device__ void merge_neighbour(const LevelArgs &A, int u, int wu, int iu, int v
     if (lane >= o) incl += y;
   }
   const int total = __shfl_sync(0xffffffffu, incl, 31);
-  const bool fits = Jn + total <= A.cap[u];
+  bool fits = Jn + total <= __ldcg(A.cap + u);
+  if (!fits && A.heap_mode) {
+    // the reference's heap adjacency is a hash map that grows freely: move the
+    // list to a fresh range (the merge writes a full new copy anyway)
+    int64_t fresh = -1;
+    const int ncap = max(2 * __ldcg(A.cap + u), Jn + total);
+    if (lane == 0) {
+      const unsigned long long at = atomicAdd(A.pool_next, (unsigned long long)ncap);
+      if ((int64_t)at + ncap <= A.pool_size) fresh = (int64_t)at;
+    }
+    fresh = __shfl_sync(0xffffffffu, fresh, 0);
+    if (fresh >= 0) {
+      off = fresh;
+      fits = true;
+      if (lane == 0) {
+        A.slot_off[u] = fresh;
+        A.cap[u] = ncap;
+      }
+    }
+  }
   if (fits) {
     int o = incl - cnt;
     int i = i0, j = k0 - i0;
@@ -181,11 +216,11 @@ __device__ void merge_neighbour(const LevelArgs &A, int u, int wu, int iu, int v
     const int ns = fits ? Jn + total : s;
     A.lsize[u] = ns;
     A.ljunk[u] = fits ? Jn : J;
-    const int h = A.height[u];
+    const int h = __ldcg(A.height + u);
     const int hn = (hnow + 1 > h) ? hnow + 1 : h;
     A.height[u] = hn;
-    const int p = A.cpos[u];
-    if (p >= 0) {  // a remaining candidate of this cell: refresh its key
+    const int p = __ldcg(A.cpos + u);
+    if (p >= 0) {  // a remaining candidate of this cell: refresh its key in the leader CTA
       cand.deg[p] = ns;
       cand.third[p] = hn;
     }
@@ -193,136 +228,166 @@ __device__ void merge_neighbour(const LevelArgs &A, int u, int wu, int iu, int v
   __syncwarp();
 }
 
-__global__ void __launch_bounds__(512) contract_level_kernel(LevelArgs A) {
+__global__ void __launch_bounds__(512) elim_kernel(ElimArgs A) {
   extern __shared__ __align__(16) unsigned char smem[];
-  const int cell = A.cell_lo + blockIdx.x;
+  cg::cluster_group cluster = cg::this_cluster();
+  const int CS = (int)cluster.num_blocks();
+  const int rank = (int)cluster.block_rank();
+  const int cell = A.cell_lo + (int)(blockIdx.x / CS);
   const int start = A.cell_start[cell];
   const int k = A.cell_count[cell];
-  if (k == 0) return;
+  if (k == 0) return;  // uniform across the cluster
   const int tid = threadIdx.x, nthr = blockDim.x;
   const int lane = tid & 31, wid = tid >> 5, nw = nthr >> 5;
 
+  // identical layout in every CTA of the cluster; the leader's keys and
+  // broadcast words are the shared copies
   unsigned char *sp = smem;
-  unsigned char *gp = (unsigned char *)A.scratch + (int64_t)blockIdx.x * A.scratch_stride;
-  auto take = [&](bool in_smem, int64_t bytes) -> void * {
+  auto take = [&](int64_t bytes) -> void * {
     bytes = (bytes + 15) & ~int64_t(15);
-    void *r;
-    if (in_smem) { r = sp; sp += bytes; } else { r = gp; gp += bytes; }
+    void *r = sp;
+    sp += bytes;
     return r;
   };
   __shared__ int s_red_sum[32], s_red_deg[32], s_red_id[32], s_red_pos[32];
-  __shared__ int s_v, s_hnow, s_c, s_stop;
-  Cand cand;
-  cand.id = (int *)take(A.keys_in_smem, sizeof(int) * A.kmax);
-  cand.deg = (int *)take(A.keys_in_smem, sizeof(int) * A.kmax);
-  cand.third = (int *)take(A.keys_in_smem, sizeof(int) * A.kmax);
-  int *aid = (int *)take(A.lists_in_smem, sizeof(int) * A.lmax);
-  int *aw = (int *)take(A.lists_in_smem, sizeof(int) * A.lmax);
-  int *pid = (int *)take(A.lists_in_smem, sizeof(int) * A.lmax * nw) + (int64_t)wid * A.lmax;
-  int *pw = (int *)take(A.lists_in_smem, sizeof(int) * A.lmax * nw) + (int64_t)wid * A.lmax;
+  __shared__ int s_bc[4];  // v, HeightNow, |own list|, stop
+  Cand mine;
+  mine.id = (int *)take(sizeof(int) * A.kmax);
+  mine.deg = (int *)take(sizeof(int) * A.kmax);
+  mine.third = (int *)take(sizeof(int) * A.kmax);
+  int *aid = (int *)take(sizeof(int) * A.lmax);
+  int *aw = (int *)take(sizeof(int) * A.lmax);
+  int *pid = (int *)take(sizeof(int) * A.lmax * nw) + (int64_t)wid * A.lmax;
+  int *pw = (int *)take(sizeof(int) * A.lmax * nw) + (int64_t)wid * A.lmax;
+  Cand lead;  // the leader's keys through distributed shared memory
+  lead.id = cluster.map_shared_rank(mine.id, 0);
+  lead.deg = cluster.map_shared_rank(mine.deg, 0);
+  lead.third = cluster.map_shared_rank(mine.third, 0);
+  const int *lead_aid = cluster.map_shared_rank(aid, 0);
+  const int *lead_aw = cluster.map_shared_rank(aw, 0);
+  const int *lead_bc = cluster.map_shared_rank(s_bc, 0);
 
-  for (int i = tid; i < k; i += nthr) {
-    const int v = A.elim[start + i];
-    cand.id[i] = v;
-    cand.deg[i] = A.deg0[v];
-    cand.third[i] = 0;
-    A.cpos[v] = i;
+  if (rank == 0) {
+    for (int i = tid; i < k; i += nthr) {
+      const int v = A.elim[start + i];
+      mine.id[i] = v;
+      mine.deg[i] = A.key_deg0[v];
+      mine.third[i] = A.key_h0 ? A.key_h0[v] : 0;
+      A.cpos[v] = i;
+    }
+    if (tid == 0) s_bc[3] = 0;
   }
-  if (tid == 0) s_stop = 0;
-  __syncthreads();
+  cluster.sync();
 
   for (int j = 0; j < k; j++) {
-    // ---- 1. argmin of (deg + height, deg, id) over candidates [j, k)
-    int bs = INT_MAX, bd = INT_MAX, bi = INT_MAX, bp = -1;
-    for (int i = j + tid; i < k; i += nthr) {
-      const int d = cand.deg[i], t = cand.third[i], id = cand.id[i];
-      if (bp < 0 || key_less(d + t, d, id, bs, bd, bi)) { bs = d + t; bd = d; bi = id; bp = i; }
-    }
-    for (int o = 16; o > 0; o >>= 1) {
-      const int os = __shfl_down_sync(0xffffffffu, bs, o), od = __shfl_down_sync(0xffffffffu, bd, o);
-      const int oi = __shfl_down_sync(0xffffffffu, bi, o), op = __shfl_down_sync(0xffffffffu, bp, o);
-      if (op >= 0 && (bp < 0 || key_less(os, od, oi, bs, bd, bi))) { bs = os; bd = od; bi = oi; bp = op; }
-    }
-    if (lane == 0) { s_red_sum[wid] = bs; s_red_deg[wid] = bd; s_red_id[wid] = bi; s_red_pos[wid] = bp; }
-    __syncthreads();
-    if (tid == 0) {
-      int rs = s_red_sum[0], rd = s_red_deg[0], ri = s_red_id[0], rp = s_red_pos[0];
-      for (int w = 1; w < nw; w++) {
-        if (s_red_pos[w] >= 0 && (rp < 0 || key_less(s_red_sum[w], s_red_deg[w], s_red_id[w], rs, rd, ri))) {
-          rs = s_red_sum[w]; rd = s_red_deg[w]; ri = s_red_id[w]; rp = s_red_pos[w];
-        }
+    if (rank == 0) {
+      // ---- 1. argmin of (deg + height, deg, id) over candidates [j, k)
+      int bs = INT_MAX, bd = INT_MAX, bi = INT_MAX, bp = -1;
+      for (int i = j + tid; i < k; i += nthr) {
+        const int d = mine.deg[i], t = mine.third[i], id = mine.id[i];
+        if (bp < 0 || key_less(d + t, d, id, bs, bd, bi)) { bs = d + t; bd = d; bi = id; bp = i; }
       }
-      // ---- 2. move the pick to position j
-      const int v = cand.id[rp];
-      const int hn = cand.third[rp];
-      if (rp != j) {
-        const int u = cand.id[j];
-        cand.id[rp] = u; cand.deg[rp] = cand.deg[j]; cand.third[rp] = cand.third[j];
-        A.cpos[u] = rp;
-        cand.id[j] = v; cand.deg[j] = rd; cand.third[j] = hn;
+      for (int o = 16; o > 0; o >>= 1) {
+        const int os = __shfl_down_sync(0xffffffffu, bs, o), od = __shfl_down_sync(0xffffffffu, bd, o);
+        const int oi = __shfl_down_sync(0xffffffffu, bi, o), op = __shfl_down_sync(0xffffffffu, bp, o);
+        if (op >= 0 && (bp < 0 || key_less(os, od, oi, bs, bd, bi))) { bs = os; bd = od; bi = oi; bp = op; }
       }
-      A.cpos[v] = -1;
-      A.elim[start + j] = v;
-      s_v = v;
-      s_hnow = hn;
-    }
-    __syncthreads();
-    const int v = s_v, hnow = s_hnow;
-    // ---- 3. own list: valid part is sorted; merge duplicates, drop junk (:338-361)
-    const int64_t voff = A.slot_off[v];
-    const int vJ = A.ljunk[v];
-    const int sv = A.lsize[v] - vJ;
-    if (sv > A.lmax) { if (tid == 0) { set_err(A.err, kErrStaging); s_stop = 1; } }
-    __syncthreads();
-    if (s_stop) return;
-    for (int i = tid; i < sv; i += nthr) {
-      aid[i] = A.slot_nbr[voff + vJ + i];
-      aw[i] = A.slot_w[voff + vJ + i];
-    }
-    __syncthreads();
-    bool dup = false;
-    for (int i = tid + 1; i < sv; i += nthr)
-      if (aid[i] == aid[i - 1]) dup = true;
-    dup = __syncthreads_or(dup);
-    if (tid == 0) {
-      int c = sv;
-      if (dup) {  // carry merge (the later entry keeps the smaller weight), then compaction
-        for (int i = 1; i < sv; i++) {
-          if (aid[i] == aid[i - 1] && aid[i] != INT_MAX) {
-            if (aw[i - 1] < aw[i]) aw[i] = aw[i - 1];
-            aid[i - 1] = INT_MAX;
+      if (lane == 0) { s_red_sum[wid] = bs; s_red_deg[wid] = bd; s_red_id[wid] = bi; s_red_pos[wid] = bp; }
+      __syncthreads();
+      if (tid == 0) {
+        int rs = s_red_sum[0], rd = s_red_deg[0], ri = s_red_id[0], rp = s_red_pos[0];
+        for (int w = 1; w < nw; w++) {
+          if (s_red_pos[w] >= 0 && (rp < 0 || key_less(s_red_sum[w], s_red_deg[w], s_red_id[w], rs, rd, ri))) {
+            rs = s_red_sum[w]; rd = s_red_deg[w]; ri = s_red_id[w]; rp = s_red_pos[w];
           }
         }
-        c = 0;
-        for (int i = 0; i < sv; i++) if (aid[i] != INT_MAX) { aid[c] = aid[i]; aw[c] = aw[i]; c++; }
+        // ---- 2. move the pick to position j
+        const int v = mine.id[rp];
+        const int hn = mine.third[rp];
+        if (rp != j) {
+          const int u = mine.id[j];
+          mine.id[rp] = u; mine.deg[rp] = mine.deg[j]; mine.third[rp] = mine.third[j];
+          A.cpos[u] = rp;
+          mine.id[j] = v; mine.deg[j] = rd; mine.third[j] = hn;
+        }
+        A.cpos[v] = -1;
+        A.elim[start + j] = v;
+        s_bc[0] = v;
+        s_bc[1] = hn;
       }
-      s_c = c;
-      if (c == 0) { set_err(A.err, kErrEmpty); s_stop = 1; }
-      else { A.lsize[v] = c; A.ljunk[v] = 0; }
-    }
-    __syncthreads();
-    if (s_stop) return;
-    const int c = s_c;
-    for (int i = tid; i < c; i += nthr) { A.slot_nbr[voff + i] = aid[i]; A.slot_w[voff + i] = aw[i]; }
-    // ---- 4. neighbours, one warp each
-    for (int i = wid; i < c; i += nw) {
-      const int u = aid[i];
-      if (A.lsize[u] - A.ljunk[u] > A.lmax) {
-        if (lane == 0) set_err(A.err, kErrStaging);
-        continue;
+      __syncthreads();
+      // ---- 3. own list: valid part is sorted; merge duplicates, drop junk (:338-361)
+      const int v = s_bc[0];
+      const int64_t voff = __ldcg(A.slot_off + v);
+      const int vJ = __ldcg(A.ljunk + v);
+      const int sv = __ldcg(A.lsize + v) - vJ;
+      if (sv <= A.lmax) {
+        for (int i = tid; i < sv; i += nthr) {
+          aid[i] = __ldcg(A.slot_nbr + voff + vJ + i);
+          aw[i] = __ldcg(A.slot_w + voff + vJ + i);
+        }
       }
-      merge_neighbour(A, u, aw[i], i, v, hnow, aid, aw, c, pid, pw, lane, cand);
+      __syncthreads();
+      bool dup = false;
+      if (sv <= A.lmax)
+        for (int i = tid + 1; i < sv; i += nthr)
+          if (aid[i] == aid[i - 1]) dup = true;
+      dup = __syncthreads_or(dup);
+      if (tid == 0) {
+        int c = sv;
+        if (sv > A.lmax) {
+          set_err(A.err, kErrStaging);
+          s_bc[3] = 1;
+        } else {
+          if (dup) {  // carry merge (the later entry keeps the smaller weight), then compaction
+            for (int i = 1; i < sv; i++) {
+              if (aid[i] == aid[i - 1] && aid[i] != INT_MAX) {
+                if (aw[i - 1] < aw[i]) aw[i] = aw[i - 1];
+                aid[i - 1] = INT_MAX;
+              }
+            }
+            c = 0;
+            for (int i = 0; i < sv; i++) if (aid[i] != INT_MAX) { aid[c] = aid[i]; aw[c] = aw[i]; c++; }
+          }
+          if (c == 0 && !A.heap_mode) { set_err(A.err, kErrEmpty); s_bc[3] = 1; }
+          else { A.lsize[v] = c; A.ljunk[v] = 0; }
+        }
+        s_bc[2] = c;
+      }
+      __syncthreads();
+      const int c = s_bc[2];
+      if (!s_bc[3])
+        for (int i = tid; i < c; i += nthr) { A.slot_nbr[voff + i] = aid[i]; A.slot_w[voff + i] = aw[i]; }
     }
-    __syncthreads();
-    // ---- 5. after the first pick every remaining key becomes live (:471-475)
-    if (j == 0) {
+    cluster.sync();
+    // ---- 4. neighbours: every warp of every CTA takes whole lists
+    const int v = lead_bc[0], hnow = lead_bc[1], c = lead_bc[2];
+    const int stop = lead_bc[3];
+    if (!stop) {
+      if (rank != 0) {
+        for (int i = tid; i < c; i += nthr) { aid[i] = lead_aid[i]; aw[i] = lead_aw[i]; }
+        __syncthreads();
+      }
+      for (int i = rank * nw + wid; i < c; i += CS * nw) {
+        const int u = aid[i];
+        if (__ldcg(A.lsize + u) - __ldcg(A.ljunk + u) > A.lmax) {
+          if (lane == 0) set_err(A.err, kErrStaging);
+          continue;
+        }
+        merge_neighbour(A, u, aw[i], i, v, hnow, aid, aw, c, pid, pw, lane, lead);
+      }
+    }
+    cluster.sync();  // no CTA leaves while a peer may still read the leader's shared memory
+    if (stop) return;
+    // ---- 5. after the first pick of a partition cell every key becomes live (:471-475)
+    if (rank == 0 && j == 0 && !A.heap_mode) {
       for (int i = 1 + tid; i < k; i += nthr) {
-        const int u = cand.id[i];
-        cand.deg[i] = A.lsize[u];
-        cand.third[i] = A.height[u];
+        const int u = mine.id[i];
+        mine.deg[i] = __ldcg(A.lsize + u);
+        mine.third[i] = __ldcg(A.height + u);
       }
+      __syncthreads();
     }
-    __syncthreads();
   }
 }
 
@@ -342,6 +407,48 @@ __global__ void scatter_adjacency_kernel(const int *adj_off, const int *adj_v, c
       }
       slot_nbr[o + k] = x;
       slot_w[o + k] = w;
+    }
+  }
+}
+
+// Lists of the heap vertices as uploadCHset builds them (Traditional_H2H.cu:
+// 43-75): valid entries in list order, first-seen entry of a duplicated
+// neighbour kept; key = (number of valid entries, duplicates included;
+// height).  One warp per vertex.
+__global__ void prepare_heap_lists_kernel(const int *verts, int nv, const int64_t *slot_off, int *slot_nbr,
+                                          int *slot_w, int *lsize, int *ljunk, const int *height, int *key_deg,
+                                          int *key_h) {
+  const int lane = threadIdx.x & 31;
+  for (int64_t t = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; t < nv;
+       t += (gridDim.x * (int64_t)blockDim.x) >> 5) {
+    const int v = verts[t];
+    const int64_t off = slot_off[v];
+    const int J = ljunk[v], s = lsize[v];
+    int c = 0;
+    for (int base = J; base < s; base += 32) {
+      const int idx = base + lane;
+      int x = INT_MAX, w = 0, prev = INT_MIN;
+      if (idx < s) {
+        x = slot_nbr[off + idx];
+        w = slot_w[off + idx];
+        if (idx > J) prev = slot_nbr[off + idx - 1];
+      }
+      __syncwarp();
+      const bool keep = idx < s && x != prev;
+      const unsigned bal = __ballot_sync(0xffffffffu, keep);
+      if (keep) {  // compaction never overtakes an unread entry: target <= source
+        const int pos = c + __popc(bal & ((1u << lane) - 1u));
+        slot_nbr[off + pos] = x;
+        slot_w[off + pos] = w;
+      }
+      c += __popc(bal);
+      __syncwarp();
+    }
+    if (lane == 0) {
+      key_deg[v] = s - J;
+      key_h[v] = height[v];
+      lsize[v] = c;
+      ljunk[v] = 0;
     }
   }
 }
@@ -372,16 +479,14 @@ T *dalloc(size_t n) {
 
 }  // namespace
 
-// Runs the partition levels H..C+1 and returns every vertex's list
-// (elimination-time lists for eliminated vertices, current lists for the
-// rest) in list order, plus the updated elimination order and heights.
-void contract_partition_levels_gpu(Graph &g, std::vector<int64_t> &lst_off, std::vector<int> &lst_nbr,
-                                   std::vector<int> &lst_w) {
+// Whole elimination on the GPU: partition levels H..C+1, then the global
+// heap over the vertices of levels <= C.  Fills g.elim (elimination order),
+// g.x_off / x_id / x_w (upper neighbours X(v)\{v} sorted by id, the lists at
+// elimination time) and g.gpu_vertices.
+void contract_gpu(Graph &g) {
   const int n = g.n;
   Clock clk;
-  // per-cell bound on list lengths during the cell's level (makeAdjcentNode's
-  // alive size + out-of-cell arcs, plus parallel-arc slack)
-  const int64_t cells = (int64_t(1) << g.H) - 1;
+  const bool trace = std::getenv("GPUH2H_TRACE") != nullptr;
   std::vector<int> level_of(n, 0);
   for (int h = g.H; h >= 1; h--) {
     const int64_t lo = (int64_t(1) << (h - 1)) - 1, hi = (int64_t(1) << h) - 2;
@@ -389,125 +494,178 @@ void contract_partition_levels_gpu(Graph &g, std::vector<int64_t> &lst_off, std:
       for (int i = 0; i < g.cell_count[c]; i++) level_of[g.elim[g.cell_start[c] + i]] = h;
   }
   std::vector<int> dup(n, 0);
-  {
-    std::vector<int> tmp;
-    for (int v = 0; v < n; v++) {
-      tmp.assign(g.adj_v.begin() + g.adj_off[v], g.adj_v.begin() + g.adj_off[v + 1]);
-      std::sort(tmp.begin(), tmp.end());
-      dup[v] = (int)(tmp.size() - (std::unique(tmp.begin(), tmp.end()) - tmp.begin()));
-    }
+  for (int v = 0; v < n; v++) {
+    const int b = g.adj_off[v], e = g.adj_off[v + 1];
+    bool sorted = true;
+    for (int i = b + 1; i < e && sorted; i++) sorted = g.adj_v[i - 1] < g.adj_v[i];
+    if (sorted) continue;  // strictly increasing: no parallel arcs
+    std::vector<int> tmp(g.adj_v.begin() + b, g.adj_v.begin() + e);
+    std::sort(tmp.begin(), tmp.end());
+    dup[v] = (int)(tmp.size() - (std::unique(tmp.begin(), tmp.end()) - tmp.begin()));
   }
-  (void)cells;
+  // global heap: the vertices of cells at levels C..1 (tail of elim)
+  int64_t heap_start = INT32_MAX;
+  for (int h = g.C; h > 0; h--) {
+    const int64_t lo = (int64_t(1) << (h - 1)) - 1, hi = (int64_t(1) << h) - 2;
+    for (int64_t c = hi; c >= lo; c--) heap_start = std::min<int64_t>(heap_start, g.cell_start[c]);
+  }
+  GH_CHECK(heap_start != INT32_MAX, H2H_ERR_ARG, "ChangeToGlobalHeight must be >= 1");
+  g.gpu_vertices = (int)heap_start;
+  const int heap_n = n - (int)heap_start;
+  long long heap_us = 0;
 
-  int *d_slot_nbr = dalloc<int>(g.lub), *d_slot_w = dalloc<int>(g.lub);
+  // slot arrays: the LUB ranges, then a pool for heap lists that outgrow theirs
+  const int64_t pool_extra = (int64_t)heap_n * std::min(heap_n, 8192) + 1024;
+  const int64_t pool_size = g.lub + pool_extra;
+  int *d_slot_nbr = dalloc<int>(pool_size), *d_slot_w = dalloc<int>(pool_size);
+  unsigned long long *d_pool_next = dalloc<unsigned long long>(1);
   int64_t *d_slot_off = dalloc<int64_t>(n);
   int *d_lsize = dalloc<int>(n), *d_cap = dalloc<int>(n), *d_height = dalloc<int>(n), *d_elim = dalloc<int>(n);
-  int *d_deg0 = dalloc<int>(n), *d_cpos = dalloc<int>(n), *d_err = dalloc<int>(1), *d_ljunk = dalloc<int>(n);
-  int *d_cell_start = dalloc<int>(g.cell_start.size()), *d_cell_count = dalloc<int>(g.cell_count.size());
+  int *d_deg0 = dalloc<int>(n), *d_h0 = dalloc<int>(n), *d_cpos = dalloc<int>(n), *d_err = dalloc<int>(1);
+  int *d_ljunk = dalloc<int>(n);
+  const int ncells_all = (int)g.cell_start.size();
+  int *d_cell_start = dalloc<int>(ncells_all + 1), *d_cell_count = dalloc<int>(ncells_all + 1);
   int *d_adj_off = dalloc<int>(n + 1), *d_adj_v = dalloc<int>(g.m), *d_adj_w = dalloc<int>(g.m);
-  char *d_scratch = nullptr;
-  int64_t scratch_bytes = 0;
+  int64_t *d_out_off = nullptr;
+  int *d_out_nbr = nullptr, *d_out_w = nullptr;
   auto cleanup = [&]() {
     cudaFree(d_slot_nbr); cudaFree(d_slot_w); cudaFree(d_slot_off); cudaFree(d_lsize); cudaFree(d_cap);
-    cudaFree(d_height); cudaFree(d_elim); cudaFree(d_deg0); cudaFree(d_cpos); cudaFree(d_err); cudaFree(d_ljunk);
-    cudaFree(d_cell_start); cudaFree(d_cell_count); cudaFree(d_adj_off); cudaFree(d_adj_v); cudaFree(d_adj_w);
-    if (d_scratch) cudaFree(d_scratch);
+    cudaFree(d_height); cudaFree(d_elim); cudaFree(d_deg0); cudaFree(d_h0); cudaFree(d_cpos); cudaFree(d_err);
+    cudaFree(d_ljunk); cudaFree(d_cell_start); cudaFree(d_cell_count); cudaFree(d_adj_off); cudaFree(d_adj_v);
+    cudaFree(d_adj_w); cudaFree(d_out_off); cudaFree(d_out_nbr); cudaFree(d_out_w); cudaFree(d_pool_next);
   };
   try {
-    std::vector<int> deg(n), minus1(n, -1), zeros(n, 0);
+    std::vector<int> deg(n), minus1(n, -1);
     for (int v = 0; v < n; v++) deg[v] = g.adj_off[v + 1] - g.adj_off[v];
+    // the heap "cell" is appended after the partition cells
+    std::vector<int> cs(g.cell_start), cc(g.cell_count);
+    cs.push_back((int)heap_start);
+    cc.push_back(heap_n);
     GH_CUDA(cudaMemcpy(d_slot_off, g.slot_off.data(), sizeof(int64_t) * n, cudaMemcpyHostToDevice));
     GH_CUDA(cudaMemcpy(d_lsize, deg.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
     GH_CUDA(cudaMemcpy(d_deg0, deg.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
     GH_CUDA(cudaMemcpy(d_cap, g.cap.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
-    GH_CUDA(cudaMemcpy(d_height, zeros.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
-    GH_CUDA(cudaMemcpy(d_ljunk, zeros.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
+    GH_CUDA(cudaMemset(d_height, 0, sizeof(int) * n));
+    GH_CUDA(cudaMemset(d_ljunk, 0, sizeof(int) * n));
     GH_CUDA(cudaMemcpy(d_cpos, minus1.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
     GH_CUDA(cudaMemcpy(d_elim, g.elim.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
-    GH_CUDA(cudaMemcpy(d_cell_start, g.cell_start.data(), sizeof(int) * g.cell_start.size(), cudaMemcpyHostToDevice));
-    GH_CUDA(cudaMemcpy(d_cell_count, g.cell_count.data(), sizeof(int) * g.cell_count.size(), cudaMemcpyHostToDevice));
+    GH_CUDA(cudaMemcpy(d_cell_start, cs.data(), sizeof(int) * cs.size(), cudaMemcpyHostToDevice));
+    GH_CUDA(cudaMemcpy(d_cell_count, cc.data(), sizeof(int) * cc.size(), cudaMemcpyHostToDevice));
     GH_CUDA(cudaMemcpy(d_adj_off, g.adj_off.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice));
     if (g.m) {
       GH_CUDA(cudaMemcpy(d_adj_v, g.adj_v.data(), sizeof(int) * g.m, cudaMemcpyHostToDevice));
       GH_CUDA(cudaMemcpy(d_adj_w, g.adj_w.data(), sizeof(int) * g.m, cudaMemcpyHostToDevice));
     }
     GH_CUDA(cudaMemset(d_err, 0, sizeof(int)));
-    scatter_adjacency_kernel<<<std::max(1, std::min(4096, (n + 255) / 256)), 256>>>(d_adj_off, d_adj_v, d_adj_w, d_slot_off,
-                                                                                   d_slot_nbr, d_slot_w, n);
+    {
+      const unsigned long long first_free = (unsigned long long)g.lub;
+      GH_CUDA(cudaMemcpy(d_pool_next, &first_free, sizeof(first_free), cudaMemcpyHostToDevice));
+    }
+    scatter_adjacency_kernel<<<std::max(1, std::min(4096, (n + 255) / 256)), 256>>>(
+        d_adj_off, d_adj_v, d_adj_w, d_slot_off, d_slot_nbr, d_slot_w, n);
     GH_CUDA(cudaGetLastError());
     GH_CUDA(cudaDeviceSynchronize());
     g.t.translate_lub = clk.us();
     clk.reset();
 
-    const int smem_dyn = enable_max_dynamic_smem(contract_level_kernel);
-    const bool trace = std::getenv("GPUH2H_TRACE") != nullptr;
+    const int smem_dyn = enable_max_dynamic_smem(elim_kernel);
+    GH_CUDA(cudaFuncSetAttribute(elim_kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
     int nsm = 0, dev = 0;
     GH_CUDA(cudaGetDevice(&dev));
     GH_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-    for (int h = g.H; h > g.C; h--) {
-      const int64_t lo = (int64_t(1) << (h - 1)) - 1, hi = (int64_t(1) << h) - 2;
-      const int ncell = (int)(hi - lo + 1);
-      int kmax = 1, lmax = 1;
-      for (int64_t c = lo; c <= hi; c++) {
-        kmax = std::max(kmax, g.cell_count[c]);
-        // members of the cell at this level: vertices whose elimination level is <= h and that lie in the cut range
-        int alive = 0;
-        for (int i = g.cut_l[c]; i < g.cut_r[c]; i++) alive += level_of[g.part_ids[i]] <= h;
-        for (int i = g.cut_l[c]; i < g.cut_r[c]; i++) {
-          int v = g.part_ids[i];
-          if (level_of[v] > h) continue;
-          int out = 0;
-          for (int e = g.adj_off[v]; e < g.adj_off[v + 1]; e++) {
-            int u = g.adj_v[e];
-            if (level_of[u] > h) continue;
-            int iu = g.id_hash[u];
-            if (iu < g.cut_l[c] || iu >= g.cut_r[c]) out++;
-          }
-          lmax = std::max(lmax, alive - 1 + out + dup[v]);
-        }
+    auto al = [](int64_t b) { return (b + 15) & ~int64_t(15); };
+    // one launch: `ncell` cells from cell index `lo`, each owned by a cluster
+    auto launch = [&](int level, int64_t lo, int ncell, int kmax, int lmax, bool heap) {
+      ElimArgs A;
+      A.slot_nbr = d_slot_nbr; A.slot_w = d_slot_w; A.slot_off = d_slot_off; A.lsize = d_lsize; A.ljunk = d_ljunk;
+      A.cap = d_cap; A.height = d_height; A.elim = d_elim; A.key_deg0 = d_deg0; A.key_h0 = heap ? d_h0 : nullptr;
+      A.cell_start = d_cell_start; A.cell_count = d_cell_count; A.cpos = d_cpos; A.err = d_err;
+      A.cell_lo = (int)lo; A.kmax = kmax; A.lmax = lmax; A.heap_mode = heap ? 1 : 0;
+      A.pool_next = d_pool_next; A.pool_size = pool_size;
+      const int64_t keys_b = 3 * al(4LL * kmax);
+      auto smem_for = [&](int nw) { return keys_b + 2 * al(4LL * lmax) + 2 * al(4LL * lmax * nw); };
+      int nw = ncell * 4 < nsm ? 16 : 8;
+      while (nw > 1 && smem_for(nw) > smem_dyn) nw >>= 1;
+      GH_CHECK(smem_for(nw) <= smem_dyn, H2H_ERR_DEVICE,
+               "elimination staging does not fit shared memory (separator too large)");
+      const int64_t smem = smem_for(nw);
+      // clusters: spread the few large cells of the top levels over many SMs
+      int cs = 1;
+      while (cs < 16 && (int64_t)ncell * cs * 2 <= nsm) cs <<= 1;
+      cudaLaunchConfig_t cfg = {};
+      cudaLaunchAttribute attr[1];
+      cfg.blockDim = dim3(nw * 32);
+      cfg.dynamicSmemBytes = (size_t)smem;
+      cfg.stream = 0;
+      for (;; cs >>= 1) {
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = cs;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        cfg.gridDim = dim3(ncell * cs);
+        if (cs == 1) break;
+        int nclusters = 0;
+        if (cudaOccupancyMaxActiveClusters(&nclusters, elim_kernel, &cfg) == cudaSuccess && nclusters > 0) break;
+        cudaGetLastError();
       }
-      LevelArgs A;
-      A.slot_nbr = d_slot_nbr; A.slot_w = d_slot_w; A.slot_off = d_slot_off; A.lsize = d_lsize; A.cap = d_cap;
-      A.height = d_height; A.elim = d_elim; A.deg0 = d_deg0; A.cell_start = d_cell_start;
-      A.cell_count = d_cell_count; A.cpos = d_cpos; A.err = d_err; A.cell_lo = (int)lo;
-      A.kmax = kmax; A.lmax = lmax; A.ljunk = d_ljunk;
-      auto al = [](int64_t b) { return (b + 15) & ~int64_t(15); };
-      const int64_t keys_b = 3 * al(sizeof(int) * (int64_t)kmax);
-      auto lists_bytes = [&](int nw) { return 2 * al(4LL * lmax) + 2 * al(4LL * lmax * nw); };
-      const int64_t budget = smem_dyn;
-      // few cells (top levels): 16 warps per cell; many cells: 8 warps, several CTAs per SM
-      int nw = ncell < nsm ? 16 : 8;
-      while (nw > 4 && keys_b + lists_bytes(nw) > budget) nw >>= 1;
-      A.keys_in_smem = 1;
-      A.lists_in_smem = 1;
-      int64_t smem = keys_b + lists_bytes(nw);
-      if (smem > budget) { A.lists_in_smem = 0; smem = keys_b; }
-      if (smem > budget) { A.keys_in_smem = 0; smem = 0; }
-      int64_t stride = (A.keys_in_smem ? 0 : keys_b) + (A.lists_in_smem ? 0 : lists_bytes(nw));
-      stride = al(stride);
-      if (stride * ncell > scratch_bytes) {
-        if (d_scratch) cudaFree(d_scratch);
-        d_scratch = nullptr;
-        scratch_bytes = stride * ncell;
-        GH_CUDA(cudaMalloc(&d_scratch, scratch_bytes));
-      }
-      A.scratch = d_scratch;
-      A.scratch_stride = stride;
       cudaEvent_t ev0 = nullptr, ev1 = nullptr;
       if (trace) { cudaEventCreate(&ev0); cudaEventCreate(&ev1); cudaEventRecord(ev0); }
-      contract_level_kernel<<<ncell, nw * 32, (size_t)smem>>>(A);
-      GH_CUDA(cudaGetLastError());
+      GH_CUDA(cudaLaunchKernelEx(&cfg, elim_kernel, A));
       if (trace) {
         cudaEventRecord(ev1);
         cudaEventSynchronize(ev1);
         float ms = 0;
         cudaEventElapsedTime(&ms, ev0, ev1);
-        std::fprintf(stderr, "[gpuh2h] contract level %d: %d cells x %d warps, kmax %d, lmax %d, smem %lld (keys %s, lists %s): %.3f ms\n",
-                     h, ncell, nw, kmax, lmax, (long long)smem, A.keys_in_smem ? "smem" : "global",
-                     A.lists_in_smem ? "smem" : "global", ms);
+        std::fprintf(stderr, "[gpuh2h] elim %s %d: %d cells x %d CTAs x %d warps, kmax %d, lmax %d, smem %lld: %.3f ms\n",
+                     heap ? "heap" : "level", level, ncell, cs, nw, kmax, lmax, (long long)smem, ms);
         cudaEventDestroy(ev0);
         cudaEventDestroy(ev1);
       }
+    };
+    for (int h = g.H; h > g.C; h--) {
+      const int64_t lo = (int64_t(1) << (h - 1)) - 1, hi = (int64_t(1) << h) - 2;
+      int kmax = 1, lmax = 1;
+      for (int64_t c = lo; c <= hi; c++) {
+        kmax = std::max(kmax, g.cell_count[c]);
+        // bound on a list during this level: alive cell members - 1 + alive
+        // out-of-cell arcs (makeAdjcentNode's count) + parallel-arc slack
+        int alive = 0;
+        for (int i = g.cut_l[c]; i < g.cut_r[c]; i++) alive += level_of[g.part_ids[i]] <= h;
+        for (int i = g.cut_l[c]; i < g.cut_r[c]; i++) {
+          const int v = g.part_ids[i];
+          if (level_of[v] > h) continue;
+          int out = 0;
+          for (int e = g.adj_off[v]; e < g.adj_off[v + 1]; e++) {
+            const int u = g.adj_v[e];
+            if (level_of[u] > h) continue;
+            const int iu = g.id_hash[u];
+            if (iu < g.cut_l[c] || iu >= g.cut_r[c]) out++;
+          }
+          lmax = std::max(lmax, alive - 1 + out + dup[v]);
+        }
+      }
+      launch(h, lo, (int)(hi - lo + 1), kmax, lmax, false);
+    }
+    // ---- global heap over levels <= C, as one cell
+    {
+      cudaEvent_t hb, he;
+      GH_CUDA(cudaEventCreate(&hb));
+      GH_CUDA(cudaEventCreate(&he));
+      GH_CUDA(cudaEventRecord(hb));
+      int *d_hverts = d_elim + heap_start;
+      prepare_heap_lists_kernel<<<std::max(1, std::min(4096, (heap_n * 32 + 255) / 256)), 256>>>(
+          d_hverts, heap_n, d_slot_off, d_slot_nbr, d_slot_w, d_lsize, d_ljunk, d_height, d_deg0, d_h0);
+      GH_CUDA(cudaGetLastError());
+      launch(0, ncells_all, 1, heap_n, std::max(1, heap_n - 1), true);
+      GH_CUDA(cudaEventRecord(he));
+      GH_CUDA(cudaEventSynchronize(he));
+      float hms = 0;
+      GH_CUDA(cudaEventElapsedTime(&hms, hb, he));
+      heap_us = (long long)(hms * 1000.0f);
+      cudaEventDestroy(hb);
+      cudaEventDestroy(he);
     }
     GH_CUDA(cudaDeviceSynchronize());
     int err = 0;
@@ -515,31 +673,29 @@ void contract_partition_levels_gpu(Graph &g, std::vector<int64_t> &lst_off, std:
     GH_CHECK(err == 0, H2H_ERR_DEVICE,
              err == kErrOverflow ? "contraction: a list outgrew its LUB capacity"
              : err == kErrEmpty ? "contraction: eliminated a vertex with an empty list (disconnected input)"
-                                 : "contraction: list outgrew the staging bound");
-    g.t.td_gpu = clk.us();
+                                : "contraction: a list outgrew the staging bound");
+    g.t.td_gpu = clk.us() - heap_us;  // partition levels
+    g.t.td_cpu = heap_us;             // global heap phase (TDInCPUTime in the reference, on the GPU here)
     clk.reset();
-    // ---- copy back order, heights and compacted lists
+    // ---- elimination order and X(v) lists back to the host
     std::vector<int> lsize(n);
-    g.height.resize(n);
     GH_CUDA(cudaMemcpy(g.elim.data(), d_elim, sizeof(int) * n, cudaMemcpyDeviceToHost));
     GH_CUDA(cudaMemcpy(lsize.data(), d_lsize, sizeof(int) * n, cudaMemcpyDeviceToHost));
-    GH_CUDA(cudaMemcpy(g.height.data(), d_height, sizeof(int) * n, cudaMemcpyDeviceToHost));
-    lst_off.assign(n + 1, 0);
-    for (int v = 0; v < n; v++) lst_off[v + 1] = lst_off[v] + lsize[v];
-    const int64_t tot = lst_off[n];
-    int64_t *d_out_off = dalloc<int64_t>(n + 1);
-    int *d_out_nbr = dalloc<int>(tot), *d_out_w = dalloc<int>(tot);
-    GH_CUDA(cudaMemcpy(d_out_off, lst_off.data(), sizeof(int64_t) * (n + 1), cudaMemcpyHostToDevice));
-    gather_lists_kernel<<<std::max(1, std::min(8192, (n * 32 + 255) / 256)), 256>>>(d_slot_off, d_lsize, d_out_off,
-                                                                                   d_slot_nbr, d_slot_w, d_out_nbr,
-                                                                                   d_out_w, n);
-    cudaError_t e1 = cudaGetLastError();
-    lst_nbr.resize(tot);
-    lst_w.resize(tot);
-    cudaError_t e2 = cudaMemcpy(lst_nbr.data(), d_out_nbr, sizeof(int) * tot, cudaMemcpyDeviceToHost);
-    cudaError_t e3 = cudaMemcpy(lst_w.data(), d_out_w, sizeof(int) * tot, cudaMemcpyDeviceToHost);
-    cudaFree(d_out_off); cudaFree(d_out_nbr); cudaFree(d_out_w);
-    GH_CUDA(e1); GH_CUDA(e2); GH_CUDA(e3);
+    g.x_off.assign(n + 1, 0);
+    for (int v = 0; v < n; v++) g.x_off[v + 1] = g.x_off[v] + lsize[v];
+    const int64_t tot = g.x_off[n];
+    d_out_off = dalloc<int64_t>(n + 1);
+    d_out_nbr = dalloc<int>(tot);
+    d_out_w = dalloc<int>(tot);
+    GH_CUDA(cudaMemcpy(d_out_off, g.x_off.data(), sizeof(int64_t) * (n + 1), cudaMemcpyHostToDevice));
+    gather_lists_kernel<<<std::max(1, std::min(8192, (n * 32 + 255) / 256)), 256>>>(
+        d_slot_off, d_lsize, d_out_off, d_slot_nbr, d_slot_w, d_out_nbr, d_out_w, n);
+    GH_CUDA(cudaGetLastError());
+    g.x_id.resize(tot);
+    g.x_w.resize(tot);
+    GH_CUDA(cudaMemcpy(g.x_id.data(), d_out_nbr, sizeof(int) * tot, cudaMemcpyDeviceToHost));
+    GH_CUDA(cudaMemcpy(g.x_w.data(), d_out_w, sizeof(int) * tot, cudaMemcpyDeviceToHost));
+    g.decomposition_size = tot + n;
     g.t.translate_back = clk.us();
   } catch (...) {
     cleanup();

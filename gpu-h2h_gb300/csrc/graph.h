@@ -87,12 +87,9 @@ struct Graph {
 // Phases (one translation unit each).
 void load_graph(Graph &g, const std::string &edge, const std::string &idf, const std::string &cut);
 void build_elimination_sets(Graph &g);                 // elim_sets.cpp
-// contract.cu: levels H..C+1; returns every vertex's list in list order
-void contract_partition_levels_gpu(Graph &g, std::vector<int64_t> &lst_off, std::vector<int> &lst_nbr,
-                                   std::vector<int> &lst_w);
-// heap.cpp: levels <= C with the global min-degree heap; fills g.x_off/x_id/x_w
-void contract_global_heap(Graph &g, const std::vector<int64_t> &lst_off, const std::vector<int> &lst_nbr,
-                          const std::vector<int> &lst_w);
+// contract.cu: partition levels H..C+1 and the global heap over levels <= C;
+// fills g.elim (elimination order) and g.x_off / x_id / x_w
+void contract_gpu(Graph &g);
 void build_tree_and_rmq(Graph &g);                     // tree.cpp
 void allocate_labels_and_bfs(Graph &g);                // tree.cpp
 void fill_labels_gpu(Graph &g);                        // labels.cu
