@@ -399,7 +399,7 @@ def main():
         "gpu_launches": args.steps,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "peak_source": peak_src, "algorithmic_bytes_per_launch": abytes,
-                     "kernel": "query_kernel<8,LCA>"},
+                     "kernel": "query_tile_kernel<LCA>"},
         "clocks": clocks,
         "cpu_baseline": cpu,
     }

@@ -83,6 +83,80 @@ __global__ void query_kernel(QArgs A) {
   }
 }
 
+// Warp-tiled batch: a warp owns 32 consecutive queries.  Phase 1: every lane
+// resolves its own query (ids, LCA through the sparse table, row bases, the
+// position range) -- 32 independent dependent-load chains in flight.  Phase
+// 2: the whole warp walks each query's positions in turn with 4-way unrolled
+// loads (position, then the two label entries) and a warp min
+// (__reduce_min_sync); the owning lane keeps the answer and the 32 answers
+// leave in one coalesced store.
+template <bool LCA_MODE>
+__global__ void __launch_bounds__(256) query_tile_kernel(QArgs A) {
+  const int lane = threadIdx.x & 31;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t tile = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; (tile << 5) < A.n; tile += nwarps) {
+    const int64_t q = (tile << 5) + lane;
+    int res = INT_MAX, len = 0;
+    int64_t pb = 0, bx = 0, by = 0;
+    if (q < A.n) {
+      const int a = __ldg(A.x + q), b = __ldg(A.y + q);
+      const bool valid = (unsigned)a < (unsigned)A.nv && (unsigned)b < (unsigned)A.nv;
+      if (!valid) {
+        res = -1;
+        atomicExch(A.bad, 1);
+      } else if (a == b) {
+        res = 0;
+      } else {
+        const int fa = __ldg(A.first + a), fb = __ldg(A.first + b);
+        bx = __ldg(A.drow + a);
+        by = __ldg(A.drow + b);
+        const int l = min(fa, fb), r = max(fa, fb);
+        const int k = 31 - __clz(r - l + 1);
+        const int i1 = __ldg(A.rmq_id + __ldg(A.rmq_hash + l) + k);
+        const int i2 = __ldg(A.rmq_id + __ldg(A.rmq_hash + r - (1 << k) + 1) + k);
+        const int d1 = __ldg(A.depth + i1), d2 = __ldg(A.depth + i2);
+        if (LCA_MODE) {
+          const int lca = d1 <= d2 ? i1 : i2;
+          pb = __ldg(A.pos_hash + lca);
+          len = (int)(__ldg(A.pos_hash + lca + 1) - pb);
+        } else {
+          len = min(d1, d2);
+        }
+      }
+    }
+    for (int s = 0; s < 32; s++) {
+      const int L = __shfl_sync(0xffffffffu, len, s);
+      if (L == 0) continue;
+      const int64_t PB = __shfl_sync(0xffffffffu, pb, s);
+      const int *rx = A.dis + __shfl_sync(0xffffffffu, bx, s);
+      const int *ry = A.dis + __shfl_sync(0xffffffffu, by, s);
+      int m = INT_MAX;
+      for (int t0 = 0; t0 < L; t0 += 128) {
+        int p[4];
+        bool ok[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+          const int t = t0 + (u << 5) + lane;
+          ok[u] = t < L;
+          p[u] = ok[u] ? (LCA_MODE ? __ldg(A.pos_pos + PB + t) : t) : 0;
+        }
+        int xv[4], yv[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+          xv[u] = ok[u] ? __ldg(rx + p[u]) : 0;
+          yv[u] = ok[u] ? __ldg(ry + p[u]) : 0;
+        }
+#pragma unroll
+        for (int u = 0; u < 4; u++)
+          if (ok[u]) m = min(m, xv[u] + yv[u]);
+      }
+      m = __reduce_min_sync(0xffffffffu, m);
+      if (lane == s) res = m;
+    }
+    if (q < A.n) A.out[q] = res;
+  }
+}
+
 }  // namespace
 
 void upload_query_index(Graph &g) {
@@ -108,12 +182,11 @@ void run_query_batch(const Graph &g, const int *x, const int *y, int *out, int64
     GH_CUDA(cudaGetDevice(&dev));
     GH_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
   }
-  constexpr int G = 8;
   const int threads = 256;
-  int64_t want = (n * G + threads - 1) / threads;
-  int blocks = (int)std::min<int64_t>(want, (int64_t)nsm * 32);
-  if (mode == H2H_QUERY_LCA) query_kernel<G, true><<<std::max(1, blocks), threads, 0, s>>>(A);
-  else query_kernel<G, false><<<std::max(1, blocks), threads, 0, s>>>(A);
+  const int64_t tiles = (n + 31) / 32;
+  const int blocks = (int)std::min<int64_t>((tiles + 7) / 8, (int64_t)nsm * 8);
+  if (mode == H2H_QUERY_LCA) query_tile_kernel<true><<<std::max(1, blocks), threads, 0, s>>>(A);
+  else query_tile_kernel<false><<<std::max(1, blocks), threads, 0, s>>>(A);
   GH_CUDA(cudaGetLastError());
 }
 
