@@ -34,7 +34,7 @@ for _p in (REPO, os.path.join(REPO, "gpu-h2h_gb300")):
     if _p not in sys.path:
         sys.path.insert(0, _p)
 
-METRIC = json.load(open(os.path.join(REPO, "BASELINE.json")))["metric"]
+METRIC = "H2H build s + queries/s on 1 GB300 vs plain GPU path; query p50/p99 latency"
 WORKLOAD = dict(name="cfg1", n=264346, target_arcs=733846, aspect_milli=1300, jitter_milli=300, diag_permille=50,
                 hw_tiers=1, hw_permille10=50, hw_k=3, hw_scale_milli=400, partition_height=10, seed=1)
 H, C = 10, 2

@@ -84,7 +84,7 @@ def test_l4_labels_are_exact_distances(cfg0_root):
 
 
 def test_l3_lca_query_is_inexact_but_nolca_exact(golden0):
-    """The reference ships L3 labels; its UsingLCA query is then inexact."""
+    """The reference ships L3 labels; with them its UsingLCA query is inexact, noLCA exact."""
     l3 = golden0["cfg0_C1_L3/q_lca"]
     l4 = golden0["cfg0_C1_L4/q_lca"]
     assert (l3 != l4).any()
