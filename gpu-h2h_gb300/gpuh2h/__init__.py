@@ -77,6 +77,8 @@ SIGNATURES = {
     "h2h_generate_road": (_i32, [C.POINTER(GenParams), _cp, _cp, C.POINTER(_i64)]),
     "h2h_gen_uniform_pairs": (_i32, [_i32, _i64, C.c_uint64, _vp, _vp]),
     "h2h_gen_local_pairs": (_i32, [_vp, _i64, _i32, C.c_uint64, _vp, _vp]),
+    "h2h_fill_labels_l4_noalloc": (_i32, [_i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i64, _vp, _i32, _i32,
+                                          _vp]),
 }
 
 _lib = None
@@ -321,3 +323,14 @@ def uniform_pairs(n_vertices: int, n: int, seed: int = 1):
 def files_for(root: str, name: str, method: int = 1):
     pre = os.path.join(root, "Partition", name, PARTITION_PREFIX[method])
     return (os.path.join(root, "Graph", "USA", name + "Edge.txt"), pre + "ID.txt", pre + "Cut.txt")
+
+
+def fill_labels_l4_noalloc(n: int, order: int, father: int, depth: int, pos_hash: int, pos_id: int, pos_pos: int,
+                           pos_w: int, dis_hash: int, total_label: int, dis: int, max_depth: int, max_sep: int,
+                           stream: int = 0):
+    """h2h_fill_labels_l4_noalloc on device pointers: the L4 label fill for
+    callers that cannot allocate device memory (scratch in a fixed on-device
+    array; see include/gpuh2h.h for the size limit)."""
+    _check(load_library().h2h_fill_labels_l4_noalloc(n, order, father, depth, pos_hash, pos_id, pos_pos, pos_w,
+                                                      dis_hash, total_label, dis, max_depth, max_sep,
+                                                      stream or None))

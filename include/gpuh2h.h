@@ -135,6 +135,27 @@ int h2h_write_contract_csv(const h2h_graph *g, const char *root);
 int h2h_write_construct_info(const h2h_graph *g, const char *root);
 int h2h_write_query_result(const h2h_graph *g, const char *root, int64_t query_number, const int64_t *times_us19);
 
+/* L4 label fill that allocates nothing.  No counterpart in the reference: it
+ * is for callers that cannot call cudaMalloc -- code running inside another
+ * framework's memory budget or capture region, or plugins that may only use
+ * the buffers their host hands them.  Every input and the output `dis` are
+ * caller-owned device buffers laid out as h2h_copy_tree / h2h_copy_bfs /
+ * h2h_copy_labels return them (order = TreeBFS, any order that lists each
+ * father before its children works; pos_w = shortcut weight of each pos
+ * entry, 0 for the node itself; dis_hash has n+1 offsets and dis_hash[n] ==
+ * total_label).  The fill's scratch lives in a fixed 32 MiB __device__ array
+ * that every GPU loading the library holds until exit, so the call takes at
+ * most n + total_label + 2 <= 8,388,608 (larger trees: H2H_ERR_ARG), and
+ * max_depth / max_sep (largest depth, largest |X(v)|-1) must fit the
+ * shared-memory staging (16*max_sep + 8*max_depth bytes).  The first call on
+ * a device looks up the array's device address (make it before any stream
+ * capture).  All calls share the array: calls that overlap on the GPU race.
+ * Runs on `stream` and waits for it before returning. */
+int h2h_fill_labels_l4_noalloc(int n, const int *order, const int *father, const int *depth,
+                               const int64_t *pos_hash, const int *pos_id, const int *pos_pos, const int *pos_w,
+                               const int64_t *dis_hash, int64_t total_label, int *dis, int max_depth, int max_sep,
+                               void *stream);
+
 #ifdef __cplusplus
 }
 #endif

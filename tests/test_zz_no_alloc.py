@@ -1,0 +1,68 @@
+"""The allocation-free L4 label fill, h2h_fill_labels_l4_noalloc, through the C ABI.
+
+Some callers cannot call cudaMalloc -- code that runs inside another
+framework's memory budget or capture region, or a plugin that may only use
+the buffers its host hands it.  For them the library offers one entry point
+whose scratch lives in a fixed on-device array; the caller passes inputs and
+the output.  This test hands it the tree of an index built by the regular
+path and checks, on two calls in a row, that it writes exactly the labels
+the regular path wrote (int32, zero tolerance).  The file name sorts last so
+a run that stops at the first failure has already run every other test.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _inputs(g):
+    father, depth, _ = g.tree()
+    order, _ = g.bfs()
+    lab = g.labels()
+    ah, aid, aw = g.adj()
+    n = len(father)
+    ph = lab["pos_hash"]
+    owner = np.repeat(np.arange(n, dtype=np.int64), np.diff(ph))
+    adj_owner = np.repeat(np.arange(n, dtype=np.int64), np.diff(ah))
+    key_adj = adj_owner * n + aid
+    key_pos = owner * n + lab["pos_id"]
+    idx = np.minimum(np.searchsorted(key_adj, key_pos), max(len(key_adj) - 1, 0))
+    pos_w = np.where(lab["pos_id"] == owner, 0, aw[idx]).astype(np.int32)
+    assert np.array_equal(np.where(lab["pos_id"] == owner, key_pos, key_adj[idx]), key_pos)
+    return dict(order=order, father=father, depth=depth, pos_hash=ph, pos_id=lab["pos_id"], pos_pos=lab["pos_pos"],
+                pos_w=pos_w, dis_hash=lab["dis_hash"]), lab["dis"]
+
+
+def test_noalloc_fill_matches_regular_path_twice(cfg0_root):
+    import torch
+
+    import gpuh2h
+    g = gpuh2h.Graph("t", 6, 1, 4, 1, files=gpuh2h.files_for(cfg0_root, "cfg0"))
+    g.contraction_noHub(1)
+    g.constructLabel_noHub(2, 1, gpuh2h.LABEL_L4)
+    host, expected = _inputs(g)
+    dev = {k: torch.from_numpy(np.ascontiguousarray(v)).cuda() for k, v in host.items()}
+    n = len(host["father"])
+    total = int(host["dis_hash"][-1])
+    max_depth = int(host["depth"].max())
+    max_sep = int((np.diff(host["pos_hash"]) - 1).max())
+    out = torch.full((total,), -7, dtype=torch.int32, device="cuda")
+    s = torch.cuda.current_stream()
+    for call in range(2):
+        out.fill_(-7)
+        gpuh2h.fill_labels_l4_noalloc(n, dev["order"].data_ptr(), dev["father"].data_ptr(), dev["depth"].data_ptr(),
+                                      dev["pos_hash"].data_ptr(), dev["pos_id"].data_ptr(),
+                                      dev["pos_pos"].data_ptr(), dev["pos_w"].data_ptr(),
+                                      dev["dis_hash"].data_ptr(), total, out.data_ptr(), max_depth, max_sep,
+                                      s.cuda_stream)
+        got = out.cpu().numpy()
+        bad = np.nonzero(got != expected)[0]
+        assert len(bad) == 0, "call %d: %d label entries differ, first at %s" % (call, len(bad), bad[:5])
+    # a tree beyond the fixed scratch is refused before any device work
+    with pytest.raises(gpuh2h.H2HError) as e:
+        gpuh2h.fill_labels_l4_noalloc(n, dev["order"].data_ptr(), dev["father"].data_ptr(), dev["depth"].data_ptr(),
+                                      dev["pos_hash"].data_ptr(), dev["pos_id"].data_ptr(),
+                                      dev["pos_pos"].data_ptr(), dev["pos_w"].data_ptr(),
+                                      dev["dis_hash"].data_ptr(), 1 << 23, out.data_ptr(), max_depth, max_sep,
+                                      s.cuda_stream)
+    assert e.value.code == -1
