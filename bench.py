@@ -149,9 +149,15 @@ def reduce_max(value: float, world: int) -> float:
         return value
     import torch
     import torch.distributed as dist
-    t = torch.tensor([value], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([value], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def rank_query_seed(rank: int) -> int:
+    """Each replica answers its own batch: seeds differ per rank."""
+    return 7 + rank
 
 
 def barrier(world: int):
@@ -271,7 +277,7 @@ def main():
         build_times.append(bt)
     info = g.info()
     phases = {k[2:-3]: info[k] / 1e3 for k in info if k.startswith("t_") and k.endswith("_us")}
-    x, y = query_pairs(g, info["n"], 7 + rank)
+    x, y = query_pairs(g, info["n"], rank_query_seed(rank))
     nq = len(x)
     xd = torch.from_numpy(x).cuda()
     yd = torch.from_numpy(y).cuda()

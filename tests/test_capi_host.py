@@ -1,0 +1,156 @@
+"""C-ABI checks that need no GPU: exported symbols, loader validation and
+error codes, state errors before a build, the workload generators and the
+G2H argument-count rule (Graph_Fundamental.cu:4-95, main.cu:244-247)."""
+import ctypes as C
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import REPO, sample13_files
+
+
+def _declared():
+    names = set()
+    for f in os.listdir(os.path.join(REPO, "include")):
+        if f.endswith(".h"):
+            src = open(os.path.join(REPO, "include", f)).read()
+            src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+            names |= set(re.findall(r"\b(h2h_\w+)\s*\(", src))
+    return names
+
+
+def test_library_exports_every_declared_symbol():
+    import gpuh2h
+    L = gpuh2h.load_library()
+    declared = _declared()
+    assert len(declared) >= 25
+    missing = [n for n in sorted(declared) if not hasattr(L, n)]
+    assert not missing, missing
+    # the Python mirror binds every declared entry point with a signature
+    assert declared <= set(gpuh2h.SIGNATURES), sorted(declared - set(gpuh2h.SIGNATURES))
+
+
+def _load(files, H=4, Cg=1, threads=2):
+    import gpuh2h
+    L = gpuh2h.load_library()
+    h = C.c_void_p()
+    rc = L.h2h_load_files(*[f.encode() for f in files], b"t", H, Cg, threads, 1, C.byref(h))
+    return rc, h
+
+
+def test_load_sample_and_state_errors():
+    import gpuh2h
+    L = gpuh2h.load_library()
+    rc, h = _load(sample13_files("Latitude"))
+    assert rc == 0 and h
+    info = gpuh2h._Info()
+    assert L.h2h_get_info(h, C.byref(info)) == 0
+    assert info.n == 13 and info.m == 44 and info.partition_height == 4
+    # accessors before h2h_contract / h2h_build_labels report a state error
+    a = np.empty(13, np.int32)
+    assert L.h2h_copy_order(h, gpuh2h._p(a)) == -4
+    assert L.h2h_copy_labels(h, None, None, None, None, None) == -4
+    assert L.h2h_query_lca_nohub(h, 0, 1) == -1
+    assert b"labels not built" in L.h2h_last_error()
+    # the CPU alternatives of the reference are outside the GPU hot path
+    assert L.h2h_contract(h, 0) == -7
+    assert L.h2h_build_labels(h, 2, 1, 4) == -4
+    L.h2h_free(h)
+
+
+def test_load_paths_follow_g2h_rules(tmp_path):
+    import shutil
+
+    import gpuh2h
+    root = str(tmp_path)
+    os.makedirs(os.path.join(root, "Graph", "USA"))
+    os.makedirs(os.path.join(root, "Partition", "13"))
+    e, i, c = sample13_files("metis")
+    shutil.copy(e, os.path.join(root, "Graph", "USA", "13Edge.txt"))
+    shutil.copy(i, os.path.join(root, "Partition", "13", "metisID.txt"))
+    shutil.copy(c, os.path.join(root, "Partition", "13", "metisCut.txt"))
+    g = gpuh2h.Graph("13", 3, 1, 2, 3, root=root)          # method 3 = metis
+    assert g.info()["n"] == 13
+    with pytest.raises(gpuh2h.H2HError) as ex:
+        gpuh2h.Graph("13", 3, 1, 2, 1, root=root)          # Latitude files are absent
+    assert ex.value.code == -2
+
+
+def _write(path, text):
+    with open(path, "w") as f:
+        f.write(text)
+
+
+@pytest.mark.parametrize("case,code", [
+    ("truncated_edge", -3), ("bad_vertex", -3), ("count_mismatch", -3), ("cut_rows", -3), ("asymmetric", -7),
+    ("disconnected", -7), ("change_height", -1), ("zero_change", -1)])
+def test_loader_rejects_bad_input(tmp_path, case, code):
+    e, i, c = sample13_files("Latitude")
+    edge, idf, cut = (open(p).read() for p in (e, i, c))
+    H, Cg = 4, 1
+    if case == "truncated_edge":
+        edge = "\n".join(edge.split("\n")[:20])
+    elif case == "bad_vertex":
+        edge = edge.replace("a 1 2 4", "a 1 99 4", 1)
+    elif case == "count_mismatch":
+        edge = edge.replace("13 44", "14 44", 1)
+    elif case == "cut_rows":
+        cut = "\n".join(cut.split("\n")[:5])
+    elif case == "asymmetric":
+        lines = edge.strip().split("\n")
+        lines = [l for l in lines[1:] if l.strip() != "a 2 1 4"]
+        edge = "13 %d\n" % len(lines) + "\n".join(lines) + "\n"
+    elif case == "disconnected":
+        lines = [l for l in edge.strip().split("\n")[1:] if not (l.split()[1] in ("13",) or l.split()[2] in ("13",))]
+        edge = "13 %d\n" % len(lines) + "\n".join(lines) + "\n"
+    elif case == "change_height":
+        Cg = 5
+    elif case == "zero_change":
+        Cg = 0
+    paths = []
+    for name, text in (("E.txt", edge), ("I.txt", idf), ("C.txt", cut)):
+        p = str(tmp_path / name)
+        _write(p, text)
+        paths.append(p)
+    rc, h = _load(paths, H, Cg)
+    assert rc == code
+    assert not h
+
+
+def test_missing_file_is_io_error(tmp_path):
+    rc, h = _load([str(tmp_path / "nope.txt")] * 3)
+    assert rc == -2
+
+
+def test_generators_are_seeded_and_in_range(cfg0_root):
+    import gpuh2h
+    x1, y1 = gpuh2h.uniform_pairs(4096, 1000, 9)
+    x2, y2 = gpuh2h.uniform_pairs(4096, 1000, 9)
+    assert np.array_equal(x1, x2) and np.array_equal(y1, y2)
+    assert x1.min() >= 0 and x1.max() < 4096
+    g = gpuh2h.Graph("cfg0", 6, 1, 2, 1, files=gpuh2h.files_for(cfg0_root, "cfg0"))
+    lx, ly = g.local_pairs(500, 20, 3)
+    assert lx.min() >= 0 and ly.max() < 4096
+    # t is reachable from s within 20 hops
+    e = gpuh2h.files_for(cfg0_root, "cfg0")[0]
+    arcs = np.loadtxt(e, skiprows=1, usecols=(1, 2), dtype=np.int64) - 1
+    adj = [[] for _ in range(4096)]
+    for a, b in arcs:
+        adj[a].append(b)
+    for s, t in zip(lx[:50], ly[:50]):
+        seen, frontier = {int(s)}, [int(s)]
+        for _ in range(20):
+            frontier = [w for v in frontier for w in adj[v] if w not in seen]
+            seen.update(frontier)
+        assert int(t) in seen
+
+
+def test_g2h_cli_argument_count_rule(tmp_path):
+    from gpuh2h import _build
+    _build.build()
+    for argv in ([], ["13"], ["13", "4", "1", "2", "1", "1", "2"]):
+        r = subprocess.run([_build.CLI] + argv, cwd=str(tmp_path), capture_output=True, timeout=60)
+        assert r.returncode == 0 and r.stdout == b"" and r.stderr == b""
