@@ -81,6 +81,7 @@ struct ElimArgs {
   int kmax;               // max candidates in a cell of this launch
   int lmax;               // bound on valid list entries in a cell of this launch
   int heap_mode;          // 1: global heap semantics (live keys, no refresh, no junk)
+  int *pstage;            // non-null: per-warp merge buffers in global memory (2*lmax ints per warp)
 };
 
 __device__ __forceinline__ void set_err(int *err, int code) { atomicCAS(err, 0, code); }
@@ -257,8 +258,15 @@ __global__ void __launch_bounds__(512) elim_kernel(ElimArgs A) {
   mine.third = (int *)take(sizeof(int) * A.kmax);
   int *aid = (int *)take(sizeof(int) * A.lmax);
   int *aw = (int *)take(sizeof(int) * A.lmax);
-  int *pid = (int *)take(sizeof(int) * A.lmax * nw) + (int64_t)wid * A.lmax;
-  int *pw = (int *)take(sizeof(int) * A.lmax * nw) + (int64_t)wid * A.lmax;
+  int *pid, *pw;
+  if (A.pstage) {  // lists too long for shared memory: this warp's slab of the global staging
+    int *slab = A.pstage + ((int64_t)blockIdx.x * nw + wid) * 2 * (int64_t)A.lmax;
+    pid = slab;
+    pw = slab + A.lmax;
+  } else {
+    pid = (int *)take(sizeof(int) * A.lmax * nw) + (int64_t)wid * A.lmax;
+    pw = (int *)take(sizeof(int) * A.lmax * nw) + (int64_t)wid * A.lmax;
+  }
   Cand lead;  // the leader's keys through distributed shared memory
   lead.id = cluster.map_shared_rank(mine.id, 0);
   lead.deg = cluster.map_shared_rank(mine.deg, 0);
@@ -487,6 +495,9 @@ void contract_gpu(Graph &g) {
   const int n = g.n;
   Clock clk;
   const bool trace = std::getenv("GPUH2H_TRACE") != nullptr;
+  // merge buffers in global memory even where shared memory would do (covers
+  // the path large separators take, on small test graphs)
+  const bool force_global_stage = std::getenv("GPUH2H_GLOBAL_STAGING") != nullptr;
   std::vector<int> level_of(n, 0);
   for (int h = g.H; h >= 1; h--) {
     const int64_t lo = (int64_t(1) << (h - 1)) - 1, hi = (int64_t(1) << h) - 2;
@@ -519,6 +530,8 @@ void contract_gpu(Graph &g) {
   const int64_t pool_size = g.lub + pool_extra;
   int *d_slot_nbr = dalloc<int>(pool_size), *d_slot_w = dalloc<int>(pool_size);
   unsigned long long *d_pool_next = dalloc<unsigned long long>(1);
+  int *d_pstage = nullptr;  // global merge staging for levels whose lists do not fit shared memory
+  int64_t pstage_ints = 0;
   int64_t *d_slot_off = dalloc<int64_t>(n);
   int *d_lsize = dalloc<int>(n), *d_cap = dalloc<int>(n), *d_height = dalloc<int>(n), *d_elim = dalloc<int>(n);
   int *d_deg0 = dalloc<int>(n), *d_h0 = dalloc<int>(n), *d_cpos = dalloc<int>(n), *d_err = dalloc<int>(1);
@@ -533,6 +546,7 @@ void contract_gpu(Graph &g) {
     cudaFree(d_height); cudaFree(d_elim); cudaFree(d_deg0); cudaFree(d_h0); cudaFree(d_cpos); cudaFree(d_err);
     cudaFree(d_ljunk); cudaFree(d_cell_start); cudaFree(d_cell_count); cudaFree(d_adj_off); cudaFree(d_adj_v);
     cudaFree(d_adj_w); cudaFree(d_out_off); cudaFree(d_out_nbr); cudaFree(d_out_w); cudaFree(d_pool_next);
+    cudaFree(d_pstage);
   };
   try {
     std::vector<int> deg(n), minus1(n, -1);
@@ -583,12 +597,16 @@ void contract_gpu(Graph &g) {
       A.cell_lo = (int)lo; A.kmax = kmax; A.lmax = lmax; A.heap_mode = heap ? 1 : 0;
       A.pool_next = d_pool_next; A.pool_size = pool_size;
       const int64_t keys_b = 3 * al(4LL * kmax);
-      auto smem_for = [&](int nw) { return keys_b + 2 * al(4LL * lmax) + 2 * al(4LL * lmax * nw); };
+      const int64_t own_b = keys_b + 2 * al(4LL * lmax);
+      auto smem_for = [&](int nw) { return own_b + 2 * al(4LL * lmax * nw); };
       int nw = ncell * 4 < nsm ? 16 : 8;
-      while (nw > 1 && smem_for(nw) > smem_dyn) nw >>= 1;
-      GH_CHECK(smem_for(nw) <= smem_dyn, H2H_ERR_DEVICE,
-               "elimination staging does not fit shared memory (separator too large)");
-      const int64_t smem = smem_for(nw);
+      while (nw > 4 && smem_for(nw) > smem_dyn) nw >>= 1;
+      // per-warp merge buffers move to global memory when they do not fit
+      const bool global_stage = smem_for(nw) > smem_dyn || force_global_stage;
+      if (global_stage) nw = ncell * 4 < nsm ? 16 : 8;
+      GH_CHECK(own_b <= smem_dyn, H2H_ERR_DEVICE,
+               "elimination staging does not fit shared memory (candidate keys + eliminated list too large)");
+      const int64_t smem = global_stage ? own_b : smem_for(nw);
       // clusters: spread the few large cells of the top levels over many SMs
       int cs = 1;
       while (cs < 16 && (int64_t)ncell * cs * 2 <= nsm) cs <<= 1;
@@ -610,6 +628,18 @@ void contract_gpu(Graph &g) {
         if (cudaOccupancyMaxActiveClusters(&nclusters, elim_kernel, &cfg) == cudaSuccess && nclusters > 0) break;
         cudaGetLastError();
       }
+      A.pstage = nullptr;
+      if (global_stage) {
+        const int64_t need = (int64_t)ncell * cs * nw * 2 * (int64_t)lmax;
+        if (need > pstage_ints) {
+          cudaFree(d_pstage);
+          d_pstage = nullptr;
+          pstage_ints = 0;
+          d_pstage = dalloc<int>(need);
+          pstage_ints = need;
+        }
+        A.pstage = d_pstage;
+      }
       cudaEvent_t ev0 = nullptr, ev1 = nullptr;
       if (trace) { cudaEventCreate(&ev0); cudaEventCreate(&ev1); cudaEventRecord(ev0); }
       GH_CUDA(cudaLaunchKernelEx(&cfg, elim_kernel, A));
@@ -618,8 +648,9 @@ void contract_gpu(Graph &g) {
         cudaEventSynchronize(ev1);
         float ms = 0;
         cudaEventElapsedTime(&ms, ev0, ev1);
-        std::fprintf(stderr, "[gpuh2h] elim %s %d: %d cells x %d CTAs x %d warps, kmax %d, lmax %d, smem %lld: %.3f ms\n",
-                     heap ? "heap" : "level", level, ncell, cs, nw, kmax, lmax, (long long)smem, ms);
+        std::fprintf(stderr, "[gpuh2h] elim %s %d: %d cells x %d CTAs x %d warps, kmax %d, lmax %d, smem %lld%s: %.3f ms\n",
+                     heap ? "heap" : "level", level, ncell, cs, nw, kmax, lmax, (long long)smem,
+                     global_stage ? " (global merge staging)" : "", ms);
         cudaEventDestroy(ev0);
         cudaEventDestroy(ev1);
       }

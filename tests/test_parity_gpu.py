@@ -147,3 +147,14 @@ def test_unsupported_cpu_paths(cfg0_root):
     with pytest.raises(gpuh2h.H2HError) as e:
         g.constructLabel_noHub(2, 0)
     assert e.value.code == -7
+
+
+def test_global_merge_staging(cfg0_root, golden0, monkeypatch):
+    """The global-memory merge buffers that large separators use give the same result."""
+    import gpuh2h
+    monkeypatch.setenv("GPUH2H_GLOBAL_STAGING", "1")
+    for C in (1, 2):
+        tag = "cfg0_C%d_L4/" % C
+        g = build(gpuh2h.files_for(cfg0_root, "cfg0"), 6, C)
+        assert np.array_equal(g.order(), golden0[tag + "order"])
+        assert np.array_equal(_sha(g.labels()["dis"]), golden0[tag + "sha256/dis"])
