@@ -89,7 +89,7 @@ class ClockSampler:
         self.p = None
 
     def start(self):
-        """Start sampling and return once the first sample is in (NVML start-up
+        """Start sampling and return once five samples are in (NVML start-up
         stays outside the timed region)."""
         import threading
         self.lines = []
@@ -100,16 +100,17 @@ class ClockSampler:
         except OSError:
             self.p = None
             return
-        first = threading.Event()
+        settled = threading.Event()
 
         def reader():
             for line in self.p.stdout:
                 self.lines.append(line)
-                first.set()
-            first.set()
+                if len(self.lines) >= 5:
+                    settled.set()
+            settled.set()
         self.t = threading.Thread(target=reader, daemon=True)
         self.t.start()
-        first.wait(timeout=20)
+        settled.wait(timeout=20)
 
     def stop(self) -> dict:
         if self.p is None:
@@ -298,6 +299,9 @@ def main():
     torch.cuda.synchronize()
     sampler.start()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    # a 20 ms device sleep ahead of the first event: every step is enqueued
+    # before the timed region starts, so a host stall cannot idle the GPU in it
+    torch.cuda._sleep(40_000_000)
     e0.record(stream)
     for _ in range(args.steps):
         g.query_device(xd.data_ptr(), yd.data_ptr(), od.data_ptr(), nq, gpuh2h.QUERY_LCA, sp)

@@ -151,6 +151,14 @@ __global__ void fill_level_kernel(FillArgs A) {
 // Each node also publishes its ancestor chain (ids of the ancestors at depth
 // 1..d-1, then itself) in a scratch array laid out like the labels, so its
 // children can locate the rows a_j without walking father pointers.
+// Bound on one dependency wait, in SM clock cycles: 2 s at 2 GHz, or
+// GPUH2H_SPIN_LIMIT_MS (profilers replay instrumented kernels much slower).
+long long spin_limit_cycles() {
+  long long ms = 2000;
+  if (const char *e = std::getenv("GPUH2H_SPIN_LIMIT_MS")) ms = std::max(1LL, std::atoll(e));
+  return ms * 2000000LL;
+}
+
 struct FlowArgs {
   // tiles in BFS node order: tile t covers columns [c0, c1) of node tile_node[t]
   // and separator members [u0, u1) of X(v)\{v}
@@ -438,7 +446,7 @@ void fill_labels_gpu(Graph &g) {
       A.done = d_done;
       A.next = d_next;
       A.err = D.err;
-      A.spin_limit = 4000000000LL;  // ~2 s of SM clock per wait
+      A.spin_limit = spin_limit_cycles();
       A.max_u = max_u;
       A.max_c = max_c;
       const int blocks = (int)std::min<int64_t>((int64_t)nsm * per_sm, ntiles);

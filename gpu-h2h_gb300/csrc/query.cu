@@ -91,7 +91,7 @@ __global__ void query_kernel(QArgs A) {
 // (__reduce_min_sync); the owning lane keeps the answer and the 32 answers
 // leave in one coalesced store.
 template <bool LCA_MODE>
-__global__ void __launch_bounds__(256) query_tile_kernel(QArgs A) {
+__global__ void __launch_bounds__(256, 8) query_tile_kernel(QArgs A) {
   const int lane = threadIdx.x & 31;
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
   for (int64_t tile = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; (tile << 5) < A.n; tile += nwarps) {
@@ -184,7 +184,15 @@ void run_query_batch(const Graph &g, const int *x, const int *y, int *out, int64
   }
   const int threads = 256;
   const int64_t tiles = (n + 31) / 32;
-  const int blocks = (int)std::min<int64_t>((tiles + 7) / 8, (int64_t)nsm * 8);
+  static int per_sm[2] = {0, 0};  // resident 256-thread blocks per SM, LCA / noLCA kernels
+  const int mi = mode == H2H_QUERY_LCA ? 0 : 1;
+  if (!per_sm[mi]) {
+    GH_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &per_sm[mi], mode == H2H_QUERY_LCA ? query_tile_kernel<true> : query_tile_kernel<false>, threads, 0));
+    per_sm[mi] = std::max(1, per_sm[mi]);
+  }
+  // one wave of resident blocks, grid-striding over the tiles
+  const int blocks = (int)std::min<int64_t>((tiles + 7) / 8, (int64_t)nsm * per_sm[mi]);
   if (mode == H2H_QUERY_LCA) query_tile_kernel<true><<<std::max(1, blocks), threads, 0, s>>>(A);
   else query_tile_kernel<false><<<std::max(1, blocks), threads, 0, s>>>(A);
   GH_CUDA(cudaGetLastError());
