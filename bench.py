@@ -389,6 +389,14 @@ def main():
                                                                  cb["labels_s"]),
                "build_s": cb["contract_s"] + cb["labels_s"]}
     pct = lambda v, q: float(np.percentile(np.asarray(v), q))
+    # L4 fill: own rows read+written, separator lists, one ancestor entry per update
+    fill_s = info["t_fill_gpu_us"] / 1e6
+    fill_bytes = 8 * info["label_size"] + 8 * info["pos_size"] + 4 * info["label_updates"]
+    fill = {"kernel": "fill_flow_kernel", "updates": info["label_updates"], "seconds": fill_s,
+            "updates_per_s": info["label_updates"] / fill_s if fill_s > 0 else None,
+            "algorithmic_bytes": fill_bytes,
+            "achieved_gbs": fill_bytes / fill_s / 1e9 if fill_s > 0 else None,
+            "frac_of_hbm": fill_bytes / fill_s / 1e9 / peak if fill_s > 0 else None}
     line = {
         "metric": METRIC, "value": value, "unit": "queries/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1000.0 * t_max / args.steps, "higher_is_better": True,
@@ -399,7 +407,7 @@ def main():
                    "queries_per_step": nq, "l2": "index %.2f GB resident > L2 (no flush)" % (info["device_bytes"] / 1e9),
                    "parallelism": "replicas x%d (queries sharded by rank)" % world},
         "build_s": statistics.median(build_times), "build_s_min": min(build_times),
-        "build_phases_ms": phases,
+        "build_phases_ms": phases, "label_fill": fill,
         "index": {"tree_height": info["tree_height"], "label_entries": info["label_size"],
                   "device_bytes": info["device_bytes"], "max_label": info["max_label"]},
         "latency_us_1e5": {"device_p50": pct(lat_dev, 50), "device_p99": pct(lat_dev, 99),

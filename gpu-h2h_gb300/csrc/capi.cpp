@@ -299,6 +299,10 @@ int h2h_get_info(const h2h_graph *h, h2h_info *info) {
   info->t_translate_labels_us = t.translate_labels;
   info->t_fill_gpu_us = t.fill_gpu;
   info->max_label = g.max_label;
+  info->label_updates = 0;
+  if (!g.pos_hash.empty() && (int)g.depth.size() == g.n)
+    for (int v = 0; v < g.n; v++)
+      info->label_updates += (g.pos_hash[v + 1] - g.pos_hash[v] - 1) * (int64_t)std::max(g.depth[v] - 2, 0);
   return H2H_OK;
 }
 

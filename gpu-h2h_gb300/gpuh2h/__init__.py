@@ -37,7 +37,7 @@ class _Info(C.Structure):
                [(f, C.c_int64) for f in ("t_load_us", "t_rank_tree_us", "t_lub_us", "t_translate_lub_us",
                                           "t_td_gpu_us", "t_translate_back_us", "t_td_cpu_us", "t_tree_us",
                                           "t_malloc_us", "t_bfs_us", "t_translate_labels_us", "t_fill_gpu_us",
-                                          "max_label")]
+                                          "max_label", "label_updates")]
 
 
 class GenParams(C.Structure):
