@@ -6,8 +6,8 @@
 #include <mutex>
 #include <string>
 
-#include "graph.h"
 #include "gpuh2h_tools.h"
+#include "handle.h"
 
 namespace gh {
 void write_partition_rate(const Graph &g, const std::string &dir);
@@ -21,44 +21,13 @@ void gen_local_pairs(const Graph &g, int64_t n, int hops, uint64_t seed, int *x,
 
 static thread_local std::string g_last_error;
 void set_last_error(const std::string &msg) { g_last_error = msg; }
-
-// Host-buffer query staging owned by a handle.
-struct HostQueryStage {
-  std::mutex mu;
-  int *dx = nullptr, *dy = nullptr, *dout = nullptr;
-  int64_t cap = 0;
-  cudaStream_t stream = nullptr;
-  ~HostQueryStage() {
-    cudaFree(dx); cudaFree(dy); cudaFree(dout);
-    if (stream) cudaStreamDestroy(stream);
-  }
-};
+const std::string &last_error() { return g_last_error; }
 
 }  // namespace gh
 
-struct h2h_graph {
-  gh::Graph g;
-  gh::HostQueryStage stage;
-};
-
 namespace {
 
-template <typename F>
-int guarded(F &&f) {
-  try {
-    f();
-    return H2H_OK;
-  } catch (const gh::Error &e) {
-    gh::set_last_error(e.what());
-    return e.code;
-  } catch (const std::bad_alloc &) {
-    gh::set_last_error("host allocation failed");
-    return H2H_ERR_NOMEM;
-  } catch (const std::exception &e) {
-    gh::set_last_error(e.what());
-    return H2H_ERR_STATE;
-  }
-}
+using gh::guarded;
 
 // Every arc u->v needs a reverse arc v->u: the partition-level kernel applies
 // the reference's pairwise fill-in per neighbour, which is the same only when
@@ -124,7 +93,7 @@ int load_common(const std::string &edge, const std::string &idf, const std::stri
 
 extern "C" {
 
-const char *h2h_last_error(void) { return gh::g_last_error.c_str(); }
+const char *h2h_last_error(void) { return gh::last_error().c_str(); }
 
 int h2h_load_files(const char *edge_file, const char *id_file, const char *cut_file, const char *graph_name,
                    int partition_height, int change_height, int thread_num, int partition_method, h2h_graph **out) {
@@ -190,7 +159,7 @@ static int single_query(const h2h_graph *h, int x, int y, int mode) {
     GH_CHECK(g.labelled, H2H_ERR_STATE, "labels not built");
     GH_CHECK(x >= 0 && x < g.n && y >= 0 && y < g.n, H2H_ERR_ARG, "vertex out of range");
     int out = 0;
-    GH_CHECK(h2h_query_batch_host(h, &x, &y, &out, 1, mode) == H2H_OK, H2H_ERR_CUDA, gh::g_last_error);
+    GH_CHECK(h2h_query_batch_host(h, &x, &y, &out, 1, mode) == H2H_OK, H2H_ERR_CUDA, gh::last_error());
     res = out;
   });
   return rc == H2H_OK ? res : -1;
@@ -356,6 +325,16 @@ int h2h_copy_labels(const h2h_graph *h, int64_t *dis_hash, int *dis, int64_t *po
     if (pos_hash) std::copy(g.pos_hash.begin(), g.pos_hash.end(), pos_hash);
     if (pos_id) std::copy(g.pos_id.begin(), g.pos_id.end(), pos_id);
     if (pos_pos) std::copy(g.pos_pos.begin(), g.pos_pos.end(), pos_pos);
+  });
+}
+
+int h2h_copy_input_arcs(const h2h_graph *h, int *adj_off, int *adj_v, int *adj_w) {
+  if (!h) { gh::set_last_error("null handle"); return H2H_ERR_ARG; }
+  return guarded([&] {
+    const gh::Graph &g = h->g;
+    if (adj_off) std::copy(g.adj_off.begin(), g.adj_off.end(), adj_off);
+    if (adj_v) std::copy(g.adj_v.begin(), g.adj_v.end(), adj_v);
+    if (adj_w) std::copy(g.adj_w.begin(), g.adj_w.end(), adj_w);
   });
 }
 

@@ -487,24 +487,25 @@ T *dalloc(size_t n) {
 
 }  // namespace
 
-// Whole elimination on the GPU: partition levels H..C+1, then the global
-// heap over the vertices of levels <= C.  Fills g.elim (elimination order),
-// g.x_off / x_id / x_w (upper neighbours X(v)\{v} sorted by id, the lists at
-// elimination time) and g.gpu_vertices.
-void contract_gpu(Graph &g) {
+namespace {
+
+// Per-graph facts the launch plan needs: the level of every vertex, the
+// parallel-arc slack of every list, and where the global order starts.
+struct GraphLevels {
+  std::vector<int> level_of, dup;
+  int heap_start = 0, heap_n = 0;
+};
+
+GraphLevels graph_levels(const Graph &g) {
+  GraphLevels L;
   const int n = g.n;
-  Clock clk;
-  const bool trace = std::getenv("GPUH2H_TRACE") != nullptr;
-  // merge buffers in global memory even where shared memory would do (covers
-  // the path large separators take, on small test graphs)
-  const bool force_global_stage = std::getenv("GPUH2H_GLOBAL_STAGING") != nullptr;
-  std::vector<int> level_of(n, 0);
+  L.level_of.assign(n, 0);
   for (int h = g.H; h >= 1; h--) {
     const int64_t lo = (int64_t(1) << (h - 1)) - 1, hi = (int64_t(1) << h) - 2;
     for (int64_t c = lo; c <= hi; c++)
-      for (int i = 0; i < g.cell_count[c]; i++) level_of[g.elim[g.cell_start[c] + i]] = h;
+      for (int i = 0; i < g.cell_count[c]; i++) L.level_of[g.elim[g.cell_start[c] + i]] = h;
   }
-  std::vector<int> dup(n, 0);
+  L.dup.assign(n, 0);
   for (int v = 0; v < n; v++) {
     const int b = g.adj_off[v], e = g.adj_off[v + 1];
     bool sorted = true;
@@ -512,227 +513,397 @@ void contract_gpu(Graph &g) {
     if (sorted) continue;  // strictly increasing: no parallel arcs
     std::vector<int> tmp(g.adj_v.begin() + b, g.adj_v.begin() + e);
     std::sort(tmp.begin(), tmp.end());
-    dup[v] = (int)(tmp.size() - (std::unique(tmp.begin(), tmp.end()) - tmp.begin()));
+    L.dup[v] = (int)(tmp.size() - (std::unique(tmp.begin(), tmp.end()) - tmp.begin()));
   }
-  // global heap: the vertices of cells at levels C..1 (tail of elim)
+  // global order: the vertices of cells at levels C..1 (tail of elim)
   int64_t heap_start = INT32_MAX;
   for (int h = g.C; h > 0; h--) {
     const int64_t lo = (int64_t(1) << (h - 1)) - 1, hi = (int64_t(1) << h) - 2;
     for (int64_t c = hi; c >= lo; c--) heap_start = std::min<int64_t>(heap_start, g.cell_start[c]);
   }
   GH_CHECK(heap_start != INT32_MAX, H2H_ERR_ARG, "ChangeToGlobalHeight must be >= 1");
-  g.gpu_vertices = (int)heap_start;
-  const int heap_n = n - (int)heap_start;
-  long long heap_us = 0;
+  L.heap_start = (int)heap_start;
+  L.heap_n = n - (int)heap_start;
+  return L;
+}
 
-  // slot arrays: the LUB ranges, then a pool for heap lists that outgrow theirs
-  const int64_t pool_extra = (int64_t)heap_n * std::min(heap_n, 8192) + 1024;
-  const int64_t pool_size = g.lub + pool_extra;
-  int *d_slot_nbr = dalloc<int>(pool_size), *d_slot_w = dalloc<int>(pool_size);
-  unsigned long long *d_pool_next = dalloc<unsigned long long>(1);
-  int *d_pstage = nullptr;  // global merge staging for levels whose lists do not fit shared memory
+// Bound on a list of cell c while level h runs: alive cell members - 1 +
+// alive out-of-cell arcs (makeAdjcentNode's count) + parallel-arc slack.
+int cell_list_bound(const Graph &g, const GraphLevels &L, int64_t c, int h) {
+  int lmax = 1, alive = 0;
+  for (int i = g.cut_l[c]; i < g.cut_r[c]; i++) alive += L.level_of[g.part_ids[i]] <= h;
+  for (int i = g.cut_l[c]; i < g.cut_r[c]; i++) {
+    const int v = g.part_ids[i];
+    if (L.level_of[v] > h) continue;
+    int out = 0;
+    for (int e = g.adj_off[v]; e < g.adj_off[v + 1]; e++) {
+      const int u = g.adj_v[e];
+      if (L.level_of[u] > h) continue;
+      const int iu = g.id_hash[u];
+      if (iu < g.cut_l[c] || iu >= g.cut_r[c]) out++;
+    }
+    lmax = std::max(lmax, alive - 1 + out + L.dup[v]);
+  }
+  return lmax;
+}
+
+template <typename T>
+T *palloc(size_t n, int64_t &bytes) {
+  T *p = dalloc<T>(n);
+  bytes += (int64_t)(std::max<size_t>(n, 1) * sizeof(T));
+  return p;
+}
+
+}  // namespace
+
+ElimPlan::ElimPlan(const std::vector<Graph *> &graphs) : gs(graphs) {
+  const int K = (int)gs.size();
+  GH_CHECK(K >= 1, H2H_ERR_ARG, "no graph to contract");
+  const bool force_global_stage = std::getenv("GPUH2H_GLOBAL_STAGING") != nullptr;
+  std::vector<GraphLevels> L(K);
+  std::vector<int64_t> lbase(K);
+  vbase.assign(K, 0);
+  mbase.assign(K, 0);
+  int64_t pool_extra = 1024;
+  for (int i = 0; i < K; i++) {
+    Graph &g = *gs[i];
+    L[i] = graph_levels(g);
+    vbase[i] = N;
+    mbase[i] = M;
+    lbase[i] = lub;
+    GH_CHECK((int64_t)N + g.n < INT32_MAX, H2H_ERR_ARG, "too many vertices in one batch");
+    N += g.n;
+    M += g.m;
+    lub += g.lub;
+    heap_total += L[i].heap_n;
+    pool_extra += (int64_t)L[i].heap_n * std::min(L[i].heap_n, 8192);
+    g.gpu_vertices = L[i].heap_start;
+  }
+  // slot arrays: the LUB ranges, then a pool for global-order lists that
+  // outgrow theirs
+  pool_size = lub + pool_extra;
+  // ---- forest arrays
+  std::vector<int64_t> f_slot_off(N);
+  std::vector<int> f_deg(N), f_cap(N), f_elim(N), f_adj_off(N + 1), f_adj_v(std::max<int64_t>(M, 1)),
+      f_adj_w(std::max<int64_t>(M, 1)), f_heap;
+  f_heap.reserve(heap_total);
+  for (int i = 0; i < K; i++) {
+    const Graph &g = *gs[i];
+    const int vb = vbase[i];
+    for (int v = 0; v < g.n; v++) {
+      f_slot_off[vb + v] = g.slot_off[v] + lbase[i];
+      f_deg[vb + v] = g.adj_off[v + 1] - g.adj_off[v];
+      f_cap[vb + v] = g.cap[v];
+      f_elim[vb + v] = g.elim[v] + vb;
+      f_adj_off[vb + v] = g.adj_off[v] + (int)mbase[i];
+    }
+    for (int64_t e = 0; e < g.m; e++) {
+      f_adj_v[mbase[i] + e] = g.adj_v[e] + vb;
+      f_adj_w[mbase[i] + e] = g.adj_w[e];
+    }
+    for (int j = L[i].heap_start; j < g.n; j++) f_heap.push_back(g.elim[j] + vb);
+  }
+  GH_CHECK(M < INT32_MAX, H2H_ERR_ARG, "too many arcs in one batch");
+  f_adj_off[N] = (int)M;
+  // ---- launches: step s takes level H_i - s of every graph still above C_i
+  std::vector<int> fcs, fcc;
+  int steps = 0;
+  for (int i = 0; i < K; i++) steps = std::max(steps, gs[i]->H - gs[i]->C);
+  struct Pending { int level; int64_t lo; int ncell, kmax, lmax; bool heap; };
+  std::vector<Pending> pend;
+  for (int st = 0; st < steps; st++) {
+    Pending P{0, (int64_t)fcs.size(), 0, 1, 1, false};
+    for (int i = 0; i < K; i++) {
+      const Graph &g = *gs[i];
+      const int h = g.H - st;
+      if (h <= g.C) continue;
+      P.level = h;
+      const int64_t lo = (int64_t(1) << (h - 1)) - 1, hi = (int64_t(1) << h) - 2;
+      for (int64_t c = lo; c <= hi; c++) {
+        fcs.push_back(vbase[i] + g.cell_start[c]);
+        fcc.push_back(g.cell_count[c]);
+        P.kmax = std::max(P.kmax, g.cell_count[c]);
+        P.lmax = std::max(P.lmax, cell_list_bound(g, L[i], c, h));
+      }
+    }
+    P.ncell = (int)(fcs.size() - P.lo);
+    if (K > 1) P.level = -(st + 1);  // a step, not one graph's level
+    if (P.ncell) pend.push_back(P);
+  }
+  {
+    Pending P{0, (int64_t)fcs.size(), K, 1, 1, true};
+    for (int i = 0; i < K; i++) {
+      fcs.push_back(vbase[i] + L[i].heap_start);
+      fcc.push_back(L[i].heap_n);
+      P.kmax = std::max(P.kmax, L[i].heap_n);
+      P.lmax = std::max(P.lmax, L[i].heap_n - 1);
+    }
+    pend.push_back(P);
+  }
+  // ---- launch shapes
+  const int smem_dyn = enable_max_dynamic_smem(elim_kernel);
+  GH_CUDA(cudaFuncSetAttribute(elim_kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+  int dev = 0;
+  GH_CUDA(cudaGetDevice(&dev));
+  GH_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  auto al = [](int64_t b) { return (b + 15) & ~int64_t(15); };
   int64_t pstage_ints = 0;
-  int64_t *d_slot_off = dalloc<int64_t>(n);
-  int *d_lsize = dalloc<int>(n), *d_cap = dalloc<int>(n), *d_height = dalloc<int>(n), *d_elim = dalloc<int>(n);
-  int *d_deg0 = dalloc<int>(n), *d_h0 = dalloc<int>(n), *d_cpos = dalloc<int>(n), *d_err = dalloc<int>(1);
-  int *d_ljunk = dalloc<int>(n);
-  const int ncells_all = (int)g.cell_start.size();
-  int *d_cell_start = dalloc<int>(ncells_all + 1), *d_cell_count = dalloc<int>(ncells_all + 1);
-  int *d_adj_off = dalloc<int>(n + 1), *d_adj_v = dalloc<int>(g.m), *d_adj_w = dalloc<int>(g.m);
-  int64_t *d_out_off = nullptr;
-  int *d_out_nbr = nullptr, *d_out_w = nullptr;
-  auto cleanup = [&]() {
-    cudaFree(d_slot_nbr); cudaFree(d_slot_w); cudaFree(d_slot_off); cudaFree(d_lsize); cudaFree(d_cap);
-    cudaFree(d_height); cudaFree(d_elim); cudaFree(d_deg0); cudaFree(d_h0); cudaFree(d_cpos); cudaFree(d_err);
-    cudaFree(d_ljunk); cudaFree(d_cell_start); cudaFree(d_cell_count); cudaFree(d_adj_off); cudaFree(d_adj_v);
-    cudaFree(d_adj_w); cudaFree(d_out_off); cudaFree(d_out_nbr); cudaFree(d_out_w); cudaFree(d_pool_next);
-    cudaFree(d_pstage);
-  };
-  try {
-    std::vector<int> deg(n), minus1(n, -1);
-    for (int v = 0; v < n; v++) deg[v] = g.adj_off[v + 1] - g.adj_off[v];
-    // the heap "cell" is appended after the partition cells
-    std::vector<int> cs(g.cell_start), cc(g.cell_count);
-    cs.push_back((int)heap_start);
-    cc.push_back(heap_n);
-    GH_CUDA(cudaMemcpy(d_slot_off, g.slot_off.data(), sizeof(int64_t) * n, cudaMemcpyHostToDevice));
-    GH_CUDA(cudaMemcpy(d_lsize, deg.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
-    GH_CUDA(cudaMemcpy(d_deg0, deg.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
-    GH_CUDA(cudaMemcpy(d_cap, g.cap.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
-    GH_CUDA(cudaMemset(d_height, 0, sizeof(int) * n));
-    GH_CUDA(cudaMemset(d_ljunk, 0, sizeof(int) * n));
-    GH_CUDA(cudaMemcpy(d_cpos, minus1.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
-    GH_CUDA(cudaMemcpy(d_elim, g.elim.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
-    GH_CUDA(cudaMemcpy(d_cell_start, cs.data(), sizeof(int) * cs.size(), cudaMemcpyHostToDevice));
-    GH_CUDA(cudaMemcpy(d_cell_count, cc.data(), sizeof(int) * cc.size(), cudaMemcpyHostToDevice));
-    GH_CUDA(cudaMemcpy(d_adj_off, g.adj_off.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice));
-    if (g.m) {
-      GH_CUDA(cudaMemcpy(d_adj_v, g.adj_v.data(), sizeof(int) * g.m, cudaMemcpyHostToDevice));
-      GH_CUDA(cudaMemcpy(d_adj_w, g.adj_w.data(), sizeof(int) * g.m, cudaMemcpyHostToDevice));
-    }
-    GH_CUDA(cudaMemset(d_err, 0, sizeof(int)));
-    {
-      const unsigned long long first_free = (unsigned long long)g.lub;
-      GH_CUDA(cudaMemcpy(d_pool_next, &first_free, sizeof(first_free), cudaMemcpyHostToDevice));
-    }
-    scatter_adjacency_kernel<<<std::max(1, std::min(4096, (n + 255) / 256)), 256>>>(
-        d_adj_off, d_adj_v, d_adj_w, d_slot_off, d_slot_nbr, d_slot_w, n);
-    GH_CUDA(cudaGetLastError());
-    GH_CUDA(cudaDeviceSynchronize());
-    g.t.translate_lub = clk.us();
-    clk.reset();
-
-    const int smem_dyn = enable_max_dynamic_smem(elim_kernel);
-    GH_CUDA(cudaFuncSetAttribute(elim_kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
-    int nsm = 0, dev = 0;
-    GH_CUDA(cudaGetDevice(&dev));
-    GH_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-    auto al = [](int64_t b) { return (b + 15) & ~int64_t(15); };
-    // one launch: `ncell` cells from cell index `lo`, each owned by a cluster
-    auto launch = [&](int level, int64_t lo, int ncell, int kmax, int lmax, bool heap) {
-      ElimArgs A;
-      A.slot_nbr = d_slot_nbr; A.slot_w = d_slot_w; A.slot_off = d_slot_off; A.lsize = d_lsize; A.ljunk = d_ljunk;
-      A.cap = d_cap; A.height = d_height; A.elim = d_elim; A.key_deg0 = d_deg0; A.key_h0 = heap ? d_h0 : nullptr;
-      A.cell_start = d_cell_start; A.cell_count = d_cell_count; A.cpos = d_cpos; A.err = d_err;
-      A.cell_lo = (int)lo; A.kmax = kmax; A.lmax = lmax; A.heap_mode = heap ? 1 : 0;
-      A.pool_next = d_pool_next; A.pool_size = pool_size;
-      const int64_t keys_b = 3 * al(4LL * kmax);
-      const int64_t own_b = keys_b + 2 * al(4LL * lmax);
-      auto smem_for = [&](int nw) { return own_b + 2 * al(4LL * lmax * nw); };
-      int nw = ncell * 4 < nsm ? 16 : 8;
-      while (nw > 4 && smem_for(nw) > smem_dyn) nw >>= 1;
-      // per-warp merge buffers move to global memory when they do not fit
-      const bool global_stage = smem_for(nw) > smem_dyn || force_global_stage;
-      if (global_stage) nw = ncell * 4 < nsm ? 16 : 8;
-      GH_CHECK(own_b <= smem_dyn, H2H_ERR_DEVICE,
-               "elimination staging does not fit shared memory (candidate keys + eliminated list too large)");
-      const int64_t smem = global_stage ? own_b : smem_for(nw);
-      // clusters: spread the few large cells of the top levels over many SMs
-      int cs = 1;
-      while (cs < 16 && (int64_t)ncell * cs * 2 <= nsm) cs <<= 1;
+  for (const Pending &P : pend) {
+    Launch Lc;
+    Lc.level = P.level; Lc.lo = P.lo; Lc.ncell = P.ncell; Lc.kmax = P.kmax; Lc.lmax = P.lmax; Lc.heap = P.heap;
+    const int64_t keys_b = 3 * al(4LL * P.kmax);
+    const int64_t own_b = keys_b + 2 * al(4LL * P.lmax);
+    auto smem_for = [&](int w) { return own_b + 2 * al(4LL * P.lmax * w); };
+    int nw = P.ncell * 4 < nsm ? 16 : 8;
+    while (nw > 4 && smem_for(nw) > smem_dyn) nw >>= 1;
+    // per-warp merge buffers move to global memory when they do not fit
+    Lc.global_stage = smem_for(nw) > smem_dyn || force_global_stage;
+    if (Lc.global_stage) nw = P.ncell * 4 < nsm ? 16 : 8;
+    GH_CHECK(own_b <= smem_dyn, H2H_ERR_DEVICE,
+             "elimination staging does not fit shared memory (candidate keys + eliminated list too large)");
+    Lc.smem = Lc.global_stage ? own_b : smem_for(nw);
+    Lc.nw = nw;
+    // clusters: spread the few large cells of the top levels over many SMs
+    int cs = 1;
+    while (cs < 16 && (int64_t)P.ncell * cs * 2 <= nsm) cs <<= 1;
+    for (;; cs >>= 1) {
+      if (cs == 1) break;
       cudaLaunchConfig_t cfg = {};
       cudaLaunchAttribute attr[1];
+      attr[0].id = cudaLaunchAttributeClusterDimension;
+      attr[0].val.clusterDim.x = cs;
+      attr[0].val.clusterDim.y = 1;
+      attr[0].val.clusterDim.z = 1;
+      cfg.attrs = attr;
+      cfg.numAttrs = 1;
       cfg.blockDim = dim3(nw * 32);
-      cfg.dynamicSmemBytes = (size_t)smem;
-      cfg.stream = 0;
-      for (;; cs >>= 1) {
-        attr[0].id = cudaLaunchAttributeClusterDimension;
-        attr[0].val.clusterDim.x = cs;
-        attr[0].val.clusterDim.y = 1;
-        attr[0].val.clusterDim.z = 1;
-        cfg.attrs = attr;
-        cfg.numAttrs = 1;
-        cfg.gridDim = dim3(ncell * cs);
-        if (cs == 1) break;
-        int nclusters = 0;
-        if (cudaOccupancyMaxActiveClusters(&nclusters, elim_kernel, &cfg) == cudaSuccess && nclusters > 0) break;
-        cudaGetLastError();
-      }
-      A.pstage = nullptr;
-      if (global_stage) {
-        const int64_t need = (int64_t)ncell * cs * nw * 2 * (int64_t)lmax;
-        if (need > pstage_ints) {
-          cudaFree(d_pstage);
-          d_pstage = nullptr;
-          pstage_ints = 0;
-          d_pstage = dalloc<int>(need);
-          pstage_ints = need;
-        }
-        A.pstage = d_pstage;
-      }
-      cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-      if (trace) { cudaEventCreate(&ev0); cudaEventCreate(&ev1); cudaEventRecord(ev0); }
-      GH_CUDA(cudaLaunchKernelEx(&cfg, elim_kernel, A));
-      if (trace) {
-        cudaEventRecord(ev1);
-        cudaEventSynchronize(ev1);
-        float ms = 0;
-        cudaEventElapsedTime(&ms, ev0, ev1);
-        std::fprintf(stderr, "[gpuh2h] elim %s %d: %d cells x %d CTAs x %d warps, kmax %d, lmax %d, smem %lld%s: %.3f ms\n",
-                     heap ? "heap" : "level", level, ncell, cs, nw, kmax, lmax, (long long)smem,
-                     global_stage ? " (global merge staging)" : "", ms);
-        cudaEventDestroy(ev0);
-        cudaEventDestroy(ev1);
-      }
-    };
-    for (int h = g.H; h > g.C; h--) {
-      const int64_t lo = (int64_t(1) << (h - 1)) - 1, hi = (int64_t(1) << h) - 2;
-      int kmax = 1, lmax = 1;
-      for (int64_t c = lo; c <= hi; c++) {
-        kmax = std::max(kmax, g.cell_count[c]);
-        // bound on a list during this level: alive cell members - 1 + alive
-        // out-of-cell arcs (makeAdjcentNode's count) + parallel-arc slack
-        int alive = 0;
-        for (int i = g.cut_l[c]; i < g.cut_r[c]; i++) alive += level_of[g.part_ids[i]] <= h;
-        for (int i = g.cut_l[c]; i < g.cut_r[c]; i++) {
-          const int v = g.part_ids[i];
-          if (level_of[v] > h) continue;
-          int out = 0;
-          for (int e = g.adj_off[v]; e < g.adj_off[v + 1]; e++) {
-            const int u = g.adj_v[e];
-            if (level_of[u] > h) continue;
-            const int iu = g.id_hash[u];
-            if (iu < g.cut_l[c] || iu >= g.cut_r[c]) out++;
-          }
-          lmax = std::max(lmax, alive - 1 + out + dup[v]);
-        }
-      }
-      launch(h, lo, (int)(hi - lo + 1), kmax, lmax, false);
+      cfg.dynamicSmemBytes = (size_t)Lc.smem;
+      cfg.gridDim = dim3(P.ncell * cs);
+      int nclusters = 0;
+      if (cudaOccupancyMaxActiveClusters(&nclusters, elim_kernel, &cfg) == cudaSuccess && nclusters > 0) break;
+      cudaGetLastError();
     }
-    // ---- global heap over levels <= C, as one cell
-    {
-      cudaEvent_t hb, he;
-      GH_CUDA(cudaEventCreate(&hb));
-      GH_CUDA(cudaEventCreate(&he));
-      GH_CUDA(cudaEventRecord(hb));
-      int *d_hverts = d_elim + heap_start;
-      prepare_heap_lists_kernel<<<std::max(1, std::min(4096, (heap_n * 32 + 255) / 256)), 256>>>(
-          d_hverts, heap_n, d_slot_off, d_slot_nbr, d_slot_w, d_lsize, d_ljunk, d_height, d_deg0, d_h0);
-      GH_CUDA(cudaGetLastError());
-      launch(0, ncells_all, 1, heap_n, std::max(1, heap_n - 1), true);
-      GH_CUDA(cudaEventRecord(he));
-      GH_CUDA(cudaEventSynchronize(he));
-      float hms = 0;
-      GH_CUDA(cudaEventElapsedTime(&hms, hb, he));
-      heap_us = (long long)(hms * 1000.0f);
-      cudaEventDestroy(hb);
-      cudaEventDestroy(he);
-    }
-    GH_CUDA(cudaDeviceSynchronize());
-    int err = 0;
-    GH_CUDA(cudaMemcpy(&err, d_err, sizeof(int), cudaMemcpyDeviceToHost));
-    GH_CHECK(err == 0, H2H_ERR_DEVICE,
-             err == kErrOverflow ? "contraction: a list outgrew its LUB capacity"
-             : err == kErrEmpty ? "contraction: eliminated a vertex with an empty list (disconnected input)"
-                                : "contraction: a list outgrew the staging bound");
-    g.t.td_gpu = clk.us() - heap_us;  // partition levels
-    g.t.td_cpu = heap_us;             // global heap phase (TDInCPUTime in the reference, on the GPU here)
-    clk.reset();
-    // ---- elimination order and X(v) lists back to the host
-    std::vector<int> lsize(n);
-    GH_CUDA(cudaMemcpy(g.elim.data(), d_elim, sizeof(int) * n, cudaMemcpyDeviceToHost));
-    GH_CUDA(cudaMemcpy(lsize.data(), d_lsize, sizeof(int) * n, cudaMemcpyDeviceToHost));
-    g.x_off.assign(n + 1, 0);
-    for (int v = 0; v < n; v++) g.x_off[v + 1] = g.x_off[v] + lsize[v];
-    const int64_t tot = g.x_off[n];
-    d_out_off = dalloc<int64_t>(n + 1);
-    d_out_nbr = dalloc<int>(tot);
-    d_out_w = dalloc<int>(tot);
-    GH_CUDA(cudaMemcpy(d_out_off, g.x_off.data(), sizeof(int64_t) * (n + 1), cudaMemcpyHostToDevice));
-    gather_lists_kernel<<<std::max(1, std::min(8192, (n * 32 + 255) / 256)), 256>>>(
-        d_slot_off, d_lsize, d_out_off, d_slot_nbr, d_slot_w, d_out_nbr, d_out_w, n);
-    GH_CUDA(cudaGetLastError());
-    g.x_id.resize(tot);
-    g.x_w.resize(tot);
-    GH_CUDA(cudaMemcpy(g.x_id.data(), d_out_nbr, sizeof(int) * tot, cudaMemcpyDeviceToHost));
-    GH_CUDA(cudaMemcpy(g.x_w.data(), d_out_w, sizeof(int) * tot, cudaMemcpyDeviceToHost));
-    g.decomposition_size = tot + n;
-    g.t.translate_back = clk.us();
+    Lc.cs = cs;
+    if (Lc.global_stage)
+      pstage_ints = std::max<int64_t>(pstage_ints, (int64_t)P.ncell * cs * nw * 2 * (int64_t)P.lmax);
+    launches.push_back(Lc);
+  }
+  // ---- device state
+  try {
+    slot_nbr = palloc<int>(pool_size, bytes);
+    slot_w = palloc<int>(pool_size, bytes);
+    pool_next = palloc<unsigned long long>(1, bytes);
+    pool_first = palloc<unsigned long long>(1, bytes);
+    slot_off = palloc<int64_t>(N, bytes);
+    slot_off_init = palloc<int64_t>(N, bytes);
+    lsize = palloc<int>(N, bytes);
+    cap = palloc<int>(N, bytes);
+    cap_init = palloc<int>(N, bytes);
+    height = palloc<int>(N, bytes);
+    elim = palloc<int>(N, bytes);
+    elim_init = palloc<int>(N, bytes);
+    deg0 = palloc<int>(N, bytes);
+    deg_init = palloc<int>(N, bytes);
+    h0 = palloc<int>(N, bytes);
+    cpos = palloc<int>(N, bytes);
+    err = palloc<int>(1, bytes);
+    ljunk = palloc<int>(N, bytes);
+    cell_start = palloc<int>(fcs.size(), bytes);
+    cell_count = palloc<int>(fcc.size(), bytes);
+    adj_off = palloc<int>(N + 1, bytes);
+    adj_v = palloc<int>(std::max<int64_t>(M, 1), bytes);
+    adj_w = palloc<int>(std::max<int64_t>(M, 1), bytes);
+    heap_verts = palloc<int>(std::max(heap_total, 1), bytes);
+    if (pstage_ints) pstage = palloc<int>(pstage_ints, bytes);
+    GH_CUDA(cudaMemcpy(slot_off_init, f_slot_off.data(), sizeof(int64_t) * N, cudaMemcpyHostToDevice));
+    GH_CUDA(cudaMemcpy(deg_init, f_deg.data(), sizeof(int) * N, cudaMemcpyHostToDevice));
+    GH_CUDA(cudaMemcpy(cap_init, f_cap.data(), sizeof(int) * N, cudaMemcpyHostToDevice));
+    GH_CUDA(cudaMemcpy(elim_init, f_elim.data(), sizeof(int) * N, cudaMemcpyHostToDevice));
+    GH_CUDA(cudaMemcpy(cell_start, fcs.data(), sizeof(int) * fcs.size(), cudaMemcpyHostToDevice));
+    GH_CUDA(cudaMemcpy(cell_count, fcc.data(), sizeof(int) * fcc.size(), cudaMemcpyHostToDevice));
+    GH_CUDA(cudaMemcpy(adj_off, f_adj_off.data(), sizeof(int) * (N + 1), cudaMemcpyHostToDevice));
+    GH_CUDA(cudaMemcpy(adj_v, f_adj_v.data(), sizeof(int) * f_adj_v.size(), cudaMemcpyHostToDevice));
+    GH_CUDA(cudaMemcpy(adj_w, f_adj_w.data(), sizeof(int) * f_adj_w.size(), cudaMemcpyHostToDevice));
+    if (heap_total)
+      GH_CUDA(cudaMemcpy(heap_verts, f_heap.data(), sizeof(int) * heap_total, cudaMemcpyHostToDevice));
+    const unsigned long long first_free = (unsigned long long)lub;
+    GH_CUDA(cudaMemcpy(pool_first, &first_free, sizeof(first_free), cudaMemcpyHostToDevice));
   } catch (...) {
-    cleanup();
+    release();
     throw;
   }
-  cleanup();
+}
+
+ElimPlan::~ElimPlan() { release(); }
+
+void ElimPlan::release() {
+  void *ps[] = {slot_nbr, slot_w, pool_next, pool_first, slot_off, slot_off_init, lsize, cap, cap_init, height, elim,
+                elim_init, deg0, deg_init, h0, cpos, err, ljunk, cell_start, cell_count, adj_off, adj_v, adj_w,
+                heap_verts, pstage};
+  for (void *p : ps) cudaFree(p);
+  slot_nbr = slot_w = lsize = cap = cap_init = height = elim = elim_init = deg0 = deg_init = h0 = cpos = err = ljunk = nullptr;
+  cell_start = cell_count = adj_off = adj_v = adj_w = heap_verts = pstage = nullptr;
+  slot_off = slot_off_init = nullptr;
+  pool_next = pool_first = nullptr;
+}
+
+void ElimPlan::set_weights(int gi, const int *w, cudaStream_t s) {
+  GH_CHECK(gi >= 0 && gi < (int)gs.size(), H2H_ERR_ARG, "graph index out of range");
+  const Graph &g = *gs[gi];
+  if (g.m)
+    GH_CUDA(cudaMemcpyAsync(adj_w + mbase[gi], w, sizeof(int) * g.m, cudaMemcpyHostToDevice, s));
+}
+
+void ElimPlan::enqueue(cudaStream_t s, cudaEvent_t *heap_ev, bool trace) {
+  // ---- reset to the input lists (relocation in the global order moves
+  // lists and grows their capacity)
+  GH_CUDA(cudaMemcpyAsync(slot_off, slot_off_init, sizeof(int64_t) * N, cudaMemcpyDeviceToDevice, s));
+  GH_CUDA(cudaMemcpyAsync(cap, cap_init, sizeof(int) * N, cudaMemcpyDeviceToDevice, s));
+  GH_CUDA(cudaMemcpyAsync(lsize, deg_init, sizeof(int) * N, cudaMemcpyDeviceToDevice, s));
+  GH_CUDA(cudaMemcpyAsync(deg0, deg_init, sizeof(int) * N, cudaMemcpyDeviceToDevice, s));
+  GH_CUDA(cudaMemcpyAsync(elim, elim_init, sizeof(int) * N, cudaMemcpyDeviceToDevice, s));
+  GH_CUDA(cudaMemcpyAsync(pool_next, pool_first, sizeof(unsigned long long), cudaMemcpyDeviceToDevice, s));
+  GH_CUDA(cudaMemsetAsync(height, 0, sizeof(int) * N, s));
+  GH_CUDA(cudaMemsetAsync(ljunk, 0, sizeof(int) * N, s));
+  GH_CUDA(cudaMemsetAsync(cpos, 0xff, sizeof(int) * N, s));  // -1
+  GH_CUDA(cudaMemsetAsync(err, 0, sizeof(int), s));
+  scatter_adjacency_kernel<<<std::max(1, std::min(4096, (N + 255) / 256)), 256, 0, s>>>(
+      adj_off, adj_v, adj_w, slot_off, slot_nbr, slot_w, N);
+  GH_CUDA(cudaGetLastError());
+  for (const Launch &Lc : launches) {
+    if (Lc.heap) {
+      if (heap_ev) GH_CUDA(cudaEventRecord(heap_ev[0], s));
+      if (heap_total) {
+        prepare_heap_lists_kernel<<<std::max(1, std::min(4096, (heap_total * 32 + 255) / 256)), 256, 0, s>>>(
+            heap_verts, heap_total, slot_off, slot_nbr, slot_w, lsize, ljunk, height, deg0, h0);
+        GH_CUDA(cudaGetLastError());
+      }
+    }
+    ElimArgs A;
+    A.slot_nbr = slot_nbr; A.slot_w = slot_w; A.slot_off = slot_off; A.lsize = lsize; A.ljunk = ljunk;
+    A.cap = cap; A.height = height; A.elim = elim; A.key_deg0 = deg0; A.key_h0 = Lc.heap ? h0 : nullptr;
+    A.cell_start = cell_start; A.cell_count = cell_count; A.cpos = cpos; A.err = err;
+    A.cell_lo = (int)Lc.lo; A.kmax = Lc.kmax; A.lmax = Lc.lmax; A.heap_mode = Lc.heap ? 1 : 0;
+    A.pool_next = pool_next; A.pool_size = pool_size;
+    A.pstage = Lc.global_stage ? pstage : nullptr;
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = Lc.cs;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cfg.blockDim = dim3(Lc.nw * 32);
+    cfg.dynamicSmemBytes = (size_t)Lc.smem;
+    cfg.gridDim = dim3(Lc.ncell * Lc.cs);
+    cfg.stream = s;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    if (trace) { cudaEventCreate(&ev0); cudaEventCreate(&ev1); cudaEventRecord(ev0, s); }
+    GH_CUDA(cudaLaunchKernelEx(&cfg, elim_kernel, A));
+    if (trace) {
+      cudaEventRecord(ev1, s);
+      cudaEventSynchronize(ev1);
+      float ms = 0;
+      cudaEventElapsedTime(&ms, ev0, ev1);
+      std::fprintf(stderr, "[gpuh2h] elim %s %d: %d cells x %d CTAs x %d warps, kmax %d, lmax %d, smem %lld%s: %.3f ms\n",
+                   Lc.heap ? "heap" : "level", Lc.level, Lc.ncell, Lc.cs, Lc.nw, Lc.kmax, Lc.lmax,
+                   (long long)Lc.smem, Lc.global_stage ? " (global merge staging)" : "", ms);
+      cudaEventDestroy(ev0);
+      cudaEventDestroy(ev1);
+    }
+  }
+  if (heap_ev) GH_CUDA(cudaEventRecord(heap_ev[1], s));
+}
+
+void ElimPlan::check_error() {
+  GH_CUDA(cudaDeviceSynchronize());
+  int e = 0;
+  GH_CUDA(cudaMemcpy(&e, err, sizeof(int), cudaMemcpyDeviceToHost));
+  GH_CHECK(e == 0, H2H_ERR_DEVICE,
+           e == kErrOverflow ? "contraction: a list outgrew its LUB capacity"
+           : e == kErrEmpty  ? "contraction: eliminated a vertex with an empty list (disconnected input)"
+                             : "contraction: a list outgrew the staging bound");
+}
+
+void ElimPlan::download(bool weights_only) {
+  std::vector<int> f_lsize(N);
+  GH_CUDA(cudaMemcpy(f_lsize.data(), lsize, sizeof(int) * N, cudaMemcpyDeviceToHost));
+  std::vector<int64_t> out_off(N + 1, 0);
+  for (int v = 0; v < N; v++) out_off[v + 1] = out_off[v] + f_lsize[v];
+  const int64_t tot = out_off[N];
+  int64_t tmp_bytes = 0;
+  int64_t *d_out_off = nullptr;
+  int *d_out_nbr = nullptr, *d_out_w = nullptr;
+  try {
+    d_out_off = palloc<int64_t>(N + 1, tmp_bytes);
+    d_out_nbr = palloc<int>(std::max<int64_t>(tot, 1), tmp_bytes);
+    d_out_w = palloc<int>(std::max<int64_t>(tot, 1), tmp_bytes);
+    GH_CUDA(cudaMemcpy(d_out_off, out_off.data(), sizeof(int64_t) * (N + 1), cudaMemcpyHostToDevice));
+    gather_lists_kernel<<<std::max(1, std::min(8192, (N * 32 + 255) / 256)), 256>>>(
+        slot_off, lsize, d_out_off, slot_nbr, slot_w, d_out_nbr, d_out_w, N);
+    GH_CUDA(cudaGetLastError());
+    std::vector<int> f_nbr(weights_only ? 0 : tot), f_w(tot), f_elim(weights_only ? 0 : N);
+    if (!weights_only) {
+      GH_CUDA(cudaMemcpy(f_elim.data(), elim, sizeof(int) * N, cudaMemcpyDeviceToHost));
+      GH_CUDA(cudaMemcpy(f_nbr.data(), d_out_nbr, sizeof(int) * tot, cudaMemcpyDeviceToHost));
+    }
+    GH_CUDA(cudaMemcpy(f_w.data(), d_out_w, sizeof(int) * tot, cudaMemcpyDeviceToHost));
+    for (size_t i = 0; i < gs.size(); i++) {
+      Graph &g = *gs[i];
+      const int vb = vbase[i];
+      const int64_t ob = out_off[vb];
+      if (!weights_only) {
+        for (int v = 0; v < g.n; v++) g.elim[v] = f_elim[vb + v] - vb;
+        g.x_off.assign(g.n + 1, 0);
+        for (int v = 0; v < g.n; v++) g.x_off[v + 1] = g.x_off[v] + f_lsize[vb + v];
+        const int64_t t = g.x_off[g.n];
+        g.x_id.resize(t);
+        for (int64_t k = 0; k < t; k++) g.x_id[k] = f_nbr[ob + k] - vb;
+        g.decomposition_size = t + g.n;
+      }
+      g.x_w.assign(f_w.begin() + ob, f_w.begin() + ob + (out_off[vb + g.n] - ob));
+    }
+  } catch (...) {
+    cudaFree(d_out_off); cudaFree(d_out_nbr); cudaFree(d_out_w);
+    throw;
+  }
+  cudaFree(d_out_off); cudaFree(d_out_nbr); cudaFree(d_out_w);
+}
+
+// Whole elimination of one graph on the GPU: partition levels H..C+1, then
+// the global order over the vertices of levels <= C.  Fills g.elim
+// (elimination order), g.x_off / x_id / x_w (upper neighbours X(v)\{v}
+// sorted by id, the lists at elimination time) and g.gpu_vertices.
+void contract_gpu(Graph &g) {
+  Clock clk;
+  const bool trace = std::getenv("GPUH2H_TRACE") != nullptr;
+  ElimPlan plan({&g});
+  GH_CUDA(cudaDeviceSynchronize());
+  g.t.translate_lub = clk.us();
+  clk.reset();
+  cudaEvent_t ev[2];
+  GH_CUDA(cudaEventCreate(&ev[0]));
+  GH_CUDA(cudaEventCreate(&ev[1]));
+  long long heap_us = 0;
+  try {
+    plan.enqueue(0, ev, trace);
+    plan.check_error();
+    float hms = 0;
+    GH_CUDA(cudaEventElapsedTime(&hms, ev[0], ev[1]));
+    heap_us = (long long)(hms * 1000.0f);
+  } catch (...) {
+    cudaEventDestroy(ev[0]);
+    cudaEventDestroy(ev[1]);
+    throw;
+  }
+  cudaEventDestroy(ev[0]);
+  cudaEventDestroy(ev[1]);
+  g.t.td_gpu = clk.us() - heap_us;  // partition levels
+  g.t.td_cpu = heap_us;             // global order over levels <= C (TDInCPUTime in the reference, on the GPU here)
+  clk.reset();
+  plan.download();
+  g.t.translate_back = clk.us();
 }
 
 }  // namespace gh

@@ -3,6 +3,7 @@
 #pragma once
 
 #include <cstdint>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -13,7 +14,11 @@ namespace gh {
 // Device-resident index used by the label fill and the query kernels.
 // Label rows are padded so every row starts on a 16-byte boundary
 // (drow[v] is a multiple of 4 ints); the reference layout is restored on
-// export.  All pointers are cudaMalloc'd and owned by the handle.
+// export.  Pointers in `owned` belong to the handle.  A graph labelled in a
+// batch points into the batch's forest arrays instead (`keep` holds them):
+// depth, pos_hash, drow and father are then offset to the graph's first
+// vertex, while drow and pos_hash values stay absolute offsets into the
+// shared dis and pos_pos / pos_id arrays.
 struct DeviceIndex {
   int n = 0;
   int64_t euler = 0, rmq = 0, pos = 0, dis_padded = 0;
@@ -29,6 +34,8 @@ struct DeviceIndex {
   int *father = nullptr;      // father                 [n]
   int *err = nullptr;         // kernel error word      [1]
   int64_t bytes = 0;
+  std::vector<void *> owned;
+  std::shared_ptr<void> keep;
   void release();
 };
 
@@ -73,7 +80,8 @@ struct Graph {
   // labels (H2HConsturction.cu), reference layout on the host
   std::vector<int64_t> dis_hash, pos_hash;
   std::vector<int> pos_id, pos_pos, pos_w;  // pos_w: shortcut weight per pos entry (0 for v itself)
-  std::vector<int64_t> drow_host;           // padded device row offsets
+  std::vector<int> pos_src;                 // index of the pos entry in v's X list (-1 for v itself)
+  std::vector<int64_t> drow_host;           // padded device row offsets (absolute in a batch's forest)
   std::vector<int> tree_bfs, tree_hash;     // TreeBFS / TreeHash
   bool labelled = false;
   int64_t max_label = 0;
@@ -82,6 +90,99 @@ struct Graph {
   Timings t;
 
   ~Graph() { dev.release(); }
+};
+
+// Vertex elimination over one or more graphs in one set of launches
+// (contract.cu).  The graphs' vertices are numbered consecutively (graph i
+// starts at vbase[i]); launch s eliminates the cells of level H_i - s of
+// every graph i with H_i - s > C_i, and one last launch runs every graph's
+// global order (levels <= C_i) as one cell per graph.  The list structure
+// and the elimination order depend only on the topology, so enqueue() can be
+// replayed (or captured in a CUDA graph) after set_weights().
+struct ElimPlan {
+  struct Launch {
+    int level, ncell, kmax, lmax, cs, nw;
+    int64_t lo, smem;
+    bool heap, global_stage;
+  };
+  std::vector<Graph *> gs;
+  std::vector<int> vbase;
+  std::vector<int64_t> mbase;
+  int N = 0, heap_total = 0;
+  int64_t M = 0, lub = 0, pool_size = 0;
+  std::vector<Launch> launches;
+  int nsm = 0;
+  // device state (global vertex ids)
+  int *slot_nbr = nullptr, *slot_w = nullptr, *lsize = nullptr, *cap = nullptr, *cap_init = nullptr;
+  int *height = nullptr, *elim = nullptr;
+  int *deg0 = nullptr, *h0 = nullptr, *cpos = nullptr, *err = nullptr, *ljunk = nullptr, *cell_start = nullptr;
+  int *cell_count = nullptr, *adj_off = nullptr, *adj_v = nullptr, *adj_w = nullptr, *pstage = nullptr;
+  int *deg_init = nullptr, *elim_init = nullptr, *heap_verts = nullptr;
+  int64_t *slot_off = nullptr, *slot_off_init = nullptr;
+  unsigned long long *pool_next = nullptr, *pool_first = nullptr;
+  int64_t bytes = 0;
+  explicit ElimPlan(const std::vector<Graph *> &graphs);
+  ~ElimPlan();
+  void release();
+  ElimPlan(const ElimPlan &) = delete;
+  ElimPlan &operator=(const ElimPlan &) = delete;
+  // Resets the lists from the input arcs and runs every launch on s.  With
+  // heap_ev non-null, records heap_ev[0] before the global-order launch and
+  // heap_ev[1] after it.
+  void enqueue(cudaStream_t s, cudaEvent_t *heap_ev = nullptr, bool trace = false);
+  void check_error();  // synchronises; throws on a kernel error code
+  // Elimination order, X(v) lists and their weights back into each graph.
+  void download(bool weights_only = false);
+  void set_weights(int gi, const int *w, cudaStream_t s);  // arc weights in the graph's file order
+};
+
+// Tile shapes of the L4 dataflow fill, keyed on the width of the node's
+// tree level (below / at least the SM count) and its separator size m
+// (buckets m <= 16, <= 64, <= 256, > 256).  A node whose m * d is at most
+// small_work is one tile; a larger one is cut into col_block columns x
+// sep_chunk separator members.
+struct TilePolicy {
+  static constexpr int kWidth = 2, kSep = 4;
+  int small_work[kWidth][kSep], col_block[kWidth][kSep], sep_chunk[kWidth][kSep];
+  TilePolicy();
+  static int sep_bucket(int m) { return m <= 16 ? 0 : m <= 64 ? 1 : m <= 256 ? 2 : 3; }
+  std::string str() const;
+  bool parse(const std::string &s);
+};
+
+// The L4 label fill over one or more graphs as one forest (labels.cu): the
+// graphs' trees are laid side by side (graph i's vertex v is forest vertex
+// vbase[i] + v) and filled by one dataflow launch.  Each graph's DeviceIndex
+// becomes a view into the forest arrays.
+struct FillPlan {
+  std::vector<Graph *> gs;
+  std::vector<int> vbase;
+  int N = 0;
+  int64_t pos_total = 0, dis_total = 0;
+  TilePolicy policy;
+  std::shared_ptr<void> storage;  // forest arrays shared with the graphs' views
+  int64_t *drow = nullptr, *pos_hash = nullptr;
+  int *pos_pos = nullptr, *pos_id = nullptr, *pos_w = nullptr, *pos_src = nullptr, *father = nullptr;
+  int *depth = nullptr, *dis = nullptr;
+  // workspace
+  int *nchild = nullptr, *chain = nullptr, *done = nullptr, *next = nullptr, *err = nullptr, *tiles = nullptr;
+  int64_t ntiles = 0, tiles_cap = 0;
+  int max_u = 1, max_c = 1, blocks = 1, threads = 128;
+  size_t smem = 0;
+  int nsm = 0;
+  int64_t work_bytes = 0;
+  FillPlan(const std::vector<Graph *> &graphs, const TilePolicy &pol);
+  ~FillPlan();
+  void release_work();
+  FillPlan(const FillPlan &) = delete;
+  FillPlan &operator=(const FillPlan &) = delete;
+  void build_tiles(const TilePolicy &pol);
+  // Resets rows and flags and runs the fill on s.  With slot arrays given,
+  // the shortcut weights are first gathered from the contraction's lists
+  // (ElimPlan numbering must match); otherwise the uploaded pos_w is used.
+  void enqueue(cudaStream_t s, const int64_t *slot_off, const int *slot_w, cudaEvent_t *fill_ev = nullptr);
+  void check_error();            // synchronises; throws if a dependency wait ran out
+  void attach(bool first);       // per-graph views, max_label; first: also drow_host
 };
 
 // Phases (one translation unit each).

@@ -22,14 +22,16 @@
 #include <algorithm>
 #include <climits>
 #include <cstdlib>
+#include <sstream>
 
 #include "graph.h"
 
 namespace gh {
 
 void DeviceIndex::release() {
-  cudaFree(first); cudaFree(depth); cudaFree(rmq_hash); cudaFree(rmq_id); cudaFree(pos_hash);
-  cudaFree(pos_pos); cudaFree(pos_id); cudaFree(drow); cudaFree(dis); cudaFree(father); cudaFree(err);
+  for (void *p : owned) cudaFree(p);
+  owned.clear();
+  keep.reset();
   first = depth = rmq_id = pos_pos = pos_id = dis = father = err = nullptr;
   rmq_hash = pos_hash = drow = nullptr;
   bytes = 0;
@@ -46,6 +48,29 @@ T *dalloc(size_t n, int64_t &bytes) {
   bytes += (int64_t)(n * sizeof(T));
   return p;
 }
+
+// An allocation the handle's DeviceIndex owns.
+template <typename T>
+T *dalloc_owned(size_t n, DeviceIndex &D) {
+  T *p = dalloc<T>(n, D.bytes);
+  D.owned.push_back(p);
+  return p;
+}
+
+// Device arrays shared by the graphs of one forest fill.
+struct DevArrays {
+  std::vector<void *> p;
+  int64_t bytes = 0;
+  template <typename T>
+  T *alloc(size_t n) {
+    T *q = dalloc<T>(n, bytes);
+    p.push_back(q);
+    return q;
+  }
+  ~DevArrays() {
+    for (void *q : p) cudaFree(q);
+  }
+};
 
 // Initial rows (mallocH2HLabel_noHub, H2HConsturction.cu:636-654): INT_MAX,
 // shortcut weights at the positions of X(v), 0 at the own position.
@@ -300,12 +325,409 @@ __global__ void max_label_kernel(const int *dis, int64_t n, int *out) {
   if ((threadIdx.x & 31) == 0) atomicMax(out, m);
 }
 
+// Shortcut weights of every pos entry, read from the contraction's final
+// lists (slot_off / slot_w, forest vertex ids): entry k of v takes list
+// index pos_src[k] of v's list, or 0 for v itself.  One warp per vertex.
+__global__ void gather_pos_weights_kernel(const int64_t *pos_hash, const int *pos_src, const int64_t *slot_off,
+                                          const int *slot_w, int *pos_w, int n) {
+  const int lane = threadIdx.x & 31;
+  for (int64_t v = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; v < n;
+       v += (gridDim.x * (int64_t)blockDim.x) >> 5) {
+    const int64_t b = pos_hash[v], e = pos_hash[v + 1], so = slot_off[v];
+    for (int64_t k = b + lane; k < e; k += 32) {
+      const int src = pos_src[k];
+      pos_w[k] = src < 0 ? 0 : slot_w[so + src];
+    }
+  }
+}
+
 }  // namespace
+
+TilePolicy::TilePolicy() {
+  for (int w = 0; w < kWidth; w++)
+    for (int b = 0; b < kSep; b++) {
+      small_work[w][b] = b == kSep - 1 ? 0 : 1 << 16;  // separators above 256 members are always split
+      col_block[w][b] = 128;
+      sep_chunk[w][b] = 32;
+    }
+}
+
+std::string TilePolicy::str() const {
+  std::ostringstream o;
+  for (int w = 0; w < kWidth; w++)
+    for (int b = 0; b < kSep; b++)
+      o << (w || b ? " " : "") << small_work[w][b] << "/" << col_block[w][b] << "/" << sep_chunk[w][b];
+  return o.str();
+}
+
+bool TilePolicy::parse(const std::string &text) {
+  TilePolicy t;
+  std::istringstream in(text);
+  for (int w = 0; w < kWidth; w++)
+    for (int b = 0; b < kSep; b++) {
+      long long sw, cb, sc;
+      char s1, s2;
+      if (!(in >> sw >> s1 >> cb >> s2 >> sc) || s1 != '/' || s2 != '/') return false;
+      if (sw < 0 || sw > (1LL << 30) || cb < 1 || cb > 4096 || sc < 1 || sc > 1024) return false;
+      t.small_work[w][b] = (int)sw;
+      t.col_block[w][b] = (int)cb;
+      t.sep_chunk[w][b] = (int)sc;
+    }
+  std::string rest;
+  if (in >> rest) return false;
+  *this = t;
+  return true;
+}
+
+FillPlan::FillPlan(const std::vector<Graph *> &graphs, const TilePolicy &pol) : gs(graphs), policy(pol) {
+  const int K = (int)gs.size();
+  GH_CHECK(K >= 1, H2H_ERR_ARG, "no graph to label");
+  vbase.assign(K, 0);
+  for (int i = 0; i < K; i++) {
+    GH_CHECK((int64_t)N + gs[i]->n < INT32_MAX, H2H_ERR_ARG, "too many vertices in one batch");
+    vbase[i] = N;
+    N += gs[i]->n;
+    pos_total += gs[i]->pos_hash[gs[i]->n];
+  }
+  std::vector<int64_t> f_drow(N + 1, 0), f_pos_hash(N + 1, 0);
+  std::vector<int> f_pos_pos(pos_total), f_pos_id(pos_total), f_pos_w(pos_total), f_pos_src(pos_total);
+  std::vector<int> f_father(N), f_depth(N), f_nchild(N);
+  for (int i = 0; i < K; i++) {
+    const Graph &g = *gs[i];
+    const int vb = vbase[i];
+    const int64_t pb = f_pos_hash[vb];
+    for (int v = 0; v < g.n; v++) {
+      const int V = vb + v;
+      f_drow[V + 1] = f_drow[V] + ((g.depth[v] + 3) & ~3);
+      f_pos_hash[V + 1] = pb + g.pos_hash[v + 1];
+      f_father[V] = g.father[v] < 0 ? -1 : g.father[v] + vb;
+      f_depth[V] = g.depth[v];
+      f_nchild[V] = g.child_off[v + 1] - g.child_off[v];
+    }
+    const int64_t np = g.pos_hash[g.n];
+    for (int64_t k = 0; k < np; k++) {
+      f_pos_pos[pb + k] = g.pos_pos[k];
+      f_pos_id[pb + k] = g.pos_id[k] + vb;
+      f_pos_w[pb + k] = g.pos_w[k];
+      f_pos_src[pb + k] = g.pos_src.empty() ? -1 : g.pos_src[k];
+    }
+  }
+  dis_total = f_drow[N];
+  int dev = 0;
+  GH_CUDA(cudaGetDevice(&dev));
+  GH_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  auto st = std::make_shared<DevArrays>();
+  storage = st;
+  drow = st->alloc<int64_t>(N + 1);
+  pos_hash = st->alloc<int64_t>(N + 1);
+  pos_pos = st->alloc<int>(pos_total);
+  pos_id = st->alloc<int>(pos_total);
+  father = st->alloc<int>(N);
+  depth = st->alloc<int>(N);
+  dis = st->alloc<int>(dis_total);
+  try {
+    pos_w = dalloc<int>(pos_total, work_bytes);
+    pos_src = dalloc<int>(pos_total, work_bytes);
+    nchild = dalloc<int>(N, work_bytes);
+    chain = dalloc<int>(dis_total, work_bytes);
+    done = dalloc<int>(2 * (int64_t)N, work_bytes);  // done flags, then per-node tile counters
+    next = dalloc<int>(1, work_bytes);
+    err = dalloc<int>(1, work_bytes);
+    GH_CUDA(cudaMemcpy(drow, f_drow.data(), sizeof(int64_t) * (N + 1), cudaMemcpyHostToDevice));
+    GH_CUDA(cudaMemcpy(pos_hash, f_pos_hash.data(), sizeof(int64_t) * (N + 1), cudaMemcpyHostToDevice));
+    GH_CUDA(cudaMemcpy(pos_pos, f_pos_pos.data(), sizeof(int) * pos_total, cudaMemcpyHostToDevice));
+    GH_CUDA(cudaMemcpy(pos_id, f_pos_id.data(), sizeof(int) * pos_total, cudaMemcpyHostToDevice));
+    GH_CUDA(cudaMemcpy(pos_w, f_pos_w.data(), sizeof(int) * pos_total, cudaMemcpyHostToDevice));
+    GH_CUDA(cudaMemcpy(pos_src, f_pos_src.data(), sizeof(int) * pos_total, cudaMemcpyHostToDevice));
+    GH_CUDA(cudaMemcpy(father, f_father.data(), sizeof(int) * N, cudaMemcpyHostToDevice));
+    GH_CUDA(cudaMemcpy(depth, f_depth.data(), sizeof(int) * N, cudaMemcpyHostToDevice));
+    GH_CUDA(cudaMemcpy(nchild, f_nchild.data(), sizeof(int) * N, cudaMemcpyHostToDevice));
+    build_tiles(pol);
+  } catch (...) {
+    release_work();
+    throw;
+  }
+}
+
+FillPlan::~FillPlan() { release_work(); }
+
+void FillPlan::release_work() {
+  void *ps[] = {pos_w, pos_src, nchild, chain, done, next, err, tiles};
+  for (void *p : ps) cudaFree(p);
+  pos_w = pos_src = nchild = chain = done = next = err = tiles = nullptr;
+}
+
+// Tiles in forest BFS order (level l of every graph, then level l + 1): a
+// node's father always holds an earlier ticket, so the dataflow cannot wait
+// on work no CTA has taken.
+void FillPlan::build_tiles(const TilePolicy &pol) {
+  policy = pol;
+  int nlev = 0;
+  for (const Graph *g : gs) nlev = std::max(nlev, (int)g->tree_hash.size() - 1);
+  std::vector<int> tn, tc0, tc1, tu0, tu1, nt(N, 0);
+  max_u = 1;
+  max_c = 1;
+  for (int l = 0; l < nlev; l++) {
+    int64_t width = 0;
+    for (const Graph *g : gs)
+      if (l + 1 < (int)g->tree_hash.size()) width += g->tree_hash[l + 1] - g->tree_hash[l];
+    const int wb = width >= nsm ? 1 : 0;
+    for (size_t i = 0; i < gs.size(); i++) {
+      const Graph &g = *gs[i];
+      if (l + 1 >= (int)g.tree_hash.size()) continue;
+      for (int q = g.tree_hash[l]; q < g.tree_hash[l + 1]; q++) {
+        const int v = g.tree_bfs[q], V = vbase[i] + v, d = g.depth[v];
+        const int m = (int)(g.pos_hash[v + 1] - g.pos_hash[v]) - 1;
+        const int sb = TilePolicy::sep_bucket(m);
+        if ((int64_t)m * d <= pol.small_work[wb][sb]) {
+          tn.push_back(V); tc0.push_back(0); tc1.push_back(d); tu0.push_back(0); tu1.push_back(m);
+          nt[V] = 1;
+          max_u = std::max(max_u, m);
+          max_c = std::max(max_c, d);
+        } else {
+          const int cb = pol.col_block[wb][sb], sc = pol.sep_chunk[wb][sb];
+          for (int c = 0; c < d; c += cb)
+            for (int u = 0; u < std::max(m, 1); u += sc) {
+              tn.push_back(V); tc0.push_back(c); tc1.push_back(std::min(d, c + cb));
+              tu0.push_back(u); tu1.push_back(std::min(m, u + sc));
+              nt[V]++;
+            }
+          max_u = std::max(max_u, std::min(m, sc));
+          max_c = std::max(max_c, std::min(d, cb));
+        }
+      }
+    }
+  }
+  ntiles = (int64_t)tn.size();
+  GH_CHECK(ntiles < INT32_MAX, H2H_ERR_ARG, "too many fill tiles");
+  const int64_t need = 5 * ntiles + N;  // node, c0, c1, u0, u1, then tiles per node
+  if (need > tiles_cap) {
+    cudaFree(tiles);
+    tiles = nullptr;
+    tiles_cap = 0;
+    tiles = dalloc<int>(need, work_bytes);
+    tiles_cap = need;
+  }
+  const std::vector<int> *parts[5] = {&tn, &tc0, &tc1, &tu0, &tu1};
+  for (int k = 0; k < 5; k++)
+    GH_CUDA(cudaMemcpy(tiles + k * ntiles, parts[k]->data(), sizeof(int) * ntiles, cudaMemcpyHostToDevice));
+  GH_CUDA(cudaMemcpy(tiles + 5 * ntiles, nt.data(), sizeof(int) * N, cudaMemcpyHostToDevice));
+  const int smem_dyn = enable_max_dynamic_smem(fill_flow_kernel);
+  smem = (size_t)max_u * 16 + (size_t)max_c * 8;
+  GH_CHECK(smem <= (size_t)smem_dyn, H2H_ERR_DEVICE, "separator or tree too large for the fill staging");
+  int per_sm = 0;
+  GH_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fill_flow_kernel, threads, smem));
+  per_sm = std::max(1, per_sm);
+  blocks = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)nsm * per_sm, ntiles));
+}
+
+void FillPlan::enqueue(cudaStream_t s, const int64_t *slot_off, const int *slot_w, cudaEvent_t *fill_ev) {
+  if (slot_off) {
+    gather_pos_weights_kernel<<<std::max(1, std::min(8192, (N * 32 + 255) / 256)), 256, 0, s>>>(
+        pos_hash, pos_src, slot_off, slot_w, pos_w, N);
+    GH_CUDA(cudaGetLastError());
+  }
+  // rows start at INT_MAX: split tiles combine with atomicMin; padding stays defined
+  fill_int_kernel<<<1024, 256, 0, s>>>(dis, dis_total, INT_MAX);
+  GH_CUDA(cudaGetLastError());
+  GH_CUDA(cudaMemsetAsync(done, 0, sizeof(int) * 2 * (int64_t)N, s));
+  GH_CUDA(cudaMemsetAsync(next, 0, sizeof(int), s));
+  GH_CUDA(cudaMemsetAsync(err, 0, sizeof(int), s));
+  FlowArgs A;
+  A.tile_node = tiles;
+  A.tile_c0 = tiles + ntiles;
+  A.tile_c1 = tiles + 2 * ntiles;
+  A.tile_u0 = tiles + 3 * ntiles;
+  A.tile_u1 = tiles + 4 * ntiles;
+  A.ntiles = (int)ntiles;
+  A.node_ntiles = tiles + 5 * ntiles;
+  A.node_cnt = done + N;
+  A.father = father;
+  A.depth = depth;
+  A.nchild = nchild;
+  A.drow = drow;
+  A.dis = dis;
+  A.pos_hash = pos_hash;
+  A.pos_id = pos_id;
+  A.pos_pos = pos_pos;
+  A.pos_w = pos_w;
+  A.chain = chain;
+  A.done = done;
+  A.next = next;
+  A.err = err;
+  A.spin_limit = spin_limit_cycles();
+  A.max_u = max_u;
+  A.max_c = max_c;
+  if (fill_ev) GH_CUDA(cudaEventRecord(fill_ev[0], s));
+  fill_flow_kernel<<<blocks, threads, smem, s>>>(A);
+  GH_CUDA(cudaGetLastError());
+  if (fill_ev) GH_CUDA(cudaEventRecord(fill_ev[1], s));
+}
+
+void FillPlan::check_error() {
+  GH_CUDA(cudaDeviceSynchronize());
+  int kerr = 0;
+  GH_CUDA(cudaMemcpy(&kerr, err, sizeof(int), cudaMemcpyDeviceToHost));
+  GH_CHECK(kerr == 0, H2H_ERR_DEVICE, "label fill: a dependency wait ran out (error code " + std::to_string(kerr) + ")");
+}
+
+void FillPlan::attach(bool first) {
+  std::vector<int64_t> f_drow, f_pos_hash;
+  if (first) {
+    f_drow.resize(N + 1);
+    f_pos_hash.resize(N + 1);
+    GH_CUDA(cudaMemcpy(f_drow.data(), drow, sizeof(int64_t) * (N + 1), cudaMemcpyDeviceToHost));
+    GH_CUDA(cudaMemcpy(f_pos_hash.data(), pos_hash, sizeof(int64_t) * (N + 1), cudaMemcpyDeviceToHost));
+  }
+  for (size_t i = 0; i < gs.size(); i++) {
+    Graph &g = *gs[i];
+    DeviceIndex &D = g.dev;
+    const int vb = vbase[i];
+    if (first) {
+      D.release();
+      D.n = g.n;
+      D.keep = storage;
+      D.depth = depth + vb;
+      D.father = father + vb;
+      D.drow = drow + vb;
+      D.pos_hash = pos_hash + vb;
+      D.pos_pos = pos_pos;
+      D.pos_id = pos_id;
+      D.dis = dis;
+      D.pos = f_pos_hash[vb + g.n] - f_pos_hash[vb];
+      D.dis_padded = f_drow[vb + g.n] - f_drow[vb];
+      D.err = dalloc_owned<int>(1, D);
+      D.bytes += (int64_t)(g.n + 1) * 16 + (int64_t)g.n * 8 + D.pos * 8 + D.dis_padded * 4;
+      g.drow_host.assign(f_drow.begin() + vb, f_drow.begin() + vb + g.n + 1);
+    }
+    // largest finite label of this graph's rows
+    const int64_t r0 = g.drow_host[0], r1 = g.drow_host[g.n];
+    GH_CUDA(cudaMemset(D.err, 0, sizeof(int)));
+    max_label_kernel<<<std::max(1, std::min<int>(nsm * 4, (int)((r1 - r0 + 255) / 256))), 256>>>(dis + r0, r1 - r0,
+                                                                                                D.err);
+    GH_CUDA(cudaGetLastError());
+    int mx = 0;
+    GH_CUDA(cudaMemcpy(&mx, D.err, sizeof(int), cudaMemcpyDeviceToHost));
+    GH_CUDA(cudaMemset(D.err, 0, sizeof(int)));
+    g.max_label = mx;
+  }
+}
+
+// Autotuner of the forest fill's tile shapes.  Coordinate descent over the
+// (level width x separator size) buckets that hold nodes: for each bucket in
+// turn, first the one-tile threshold, then the column-block x separator-chunk
+// split, each candidate timed as a whole fill (best of two runs) with the
+// other buckets held; a candidate replaces the incumbent only when it is 2%
+// faster.  Any policy gives the same labels: only the schedule changes.
+std::string tile_policy_tune(FillPlan &plan, ElimPlan &elim, cudaStream_t s, int rounds) {
+  bool used[TilePolicy::kWidth][TilePolicy::kSep] = {};
+  {
+    int nlev = 0;
+    for (const Graph *g : plan.gs) nlev = std::max(nlev, (int)g->tree_hash.size() - 1);
+    for (int l = 0; l < nlev; l++) {
+      int64_t width = 0;
+      for (const Graph *g : plan.gs)
+        if (l + 1 < (int)g->tree_hash.size()) width += g->tree_hash[l + 1] - g->tree_hash[l];
+      const int wb = width >= plan.nsm ? 1 : 0;
+      for (const Graph *g : plan.gs) {
+        if (l + 1 >= (int)g->tree_hash.size()) continue;
+        for (int q = g->tree_hash[l]; q < g->tree_hash[l + 1]; q++) {
+          const int v = g->tree_bfs[q];
+          used[wb][TilePolicy::sep_bucket((int)(g->pos_hash[v + 1] - g->pos_hash[v]) - 1)] = true;
+        }
+      }
+    }
+  }
+  cudaEvent_t ev[2];
+  GH_CUDA(cudaEventCreate(&ev[0]));
+  GH_CUDA(cudaEventCreate(&ev[1]));
+  auto time_policy = [&](const TilePolicy &p) -> float {
+    try {
+      plan.build_tiles(p);
+    } catch (const Error &) {
+      return 1e30f;  // staging does not fit: not a candidate
+    }
+    float best = 1e30f;
+    for (int rep = 0; rep < 2; rep++) {
+      plan.enqueue(s, elim.slot_off, elim.slot_w, ev);
+      plan.check_error();
+      float ms = 0;
+      GH_CUDA(cudaEventElapsedTime(&ms, ev[0], ev[1]));
+      best = std::min(best, ms);
+    }
+    return best;
+  };
+  static const int kSmall[] = {0, 1 << 12, 1 << 14, 1 << 16, 1 << 18};
+  static const int kShape[][2] = {{64, 16}, {128, 16}, {128, 32}, {256, 32}, {128, 64}, {256, 64}};
+  TilePolicy best = plan.policy;
+  float best_ms = 0;
+  try {
+    best_ms = time_policy(best);
+    for (int r = 0; r < rounds; r++)
+      for (int wb = 0; wb < TilePolicy::kWidth; wb++)
+        for (int sb = 0; sb < TilePolicy::kSep; sb++) {
+          if (!used[wb][sb]) continue;
+          for (int sw : kSmall) {
+            if (sw == best.small_work[wb][sb]) continue;
+            TilePolicy p = best;
+            p.small_work[wb][sb] = sw;
+            const float t = time_policy(p);
+            if (t < best_ms * 0.98f) { best = p; best_ms = t; }
+          }
+          for (const auto &sh : kShape) {
+            if (sh[0] == best.col_block[wb][sb] && sh[1] == best.sep_chunk[wb][sb]) continue;
+            TilePolicy p = best;
+            p.col_block[wb][sb] = sh[0];
+            p.sep_chunk[wb][sb] = sh[1];
+            const float t = time_policy(p);
+            if (t < best_ms * 0.98f) { best = p; best_ms = t; }
+          }
+        }
+    time_policy(best);  // leaves the tiles and the labels of the chosen policy
+  } catch (...) {
+    cudaEventDestroy(ev[0]);
+    cudaEventDestroy(ev[1]);
+    throw;
+  }
+  cudaEventDestroy(ev[0]);
+  cudaEventDestroy(ev[1]);
+  return best.str();
+}
 
 void fill_labels_gpu(Graph &g) {
   Clock clk;
   const int n = g.n;
   DeviceIndex &D = g.dev;
+  // L4 runs as a dataflow over the tree; L3 (order-dependent, as shipped)
+  // keeps the level-synchronous kernel that applies the reference's order.
+  const bool flow = g.label_mode == H2H_LABEL_L4 && !std::getenv("GPUH2H_LEVEL_FILL");
+  if (flow) {
+    TilePolicy pol;
+    if (const char *e = std::getenv("GPUH2H_TILE_POLICY"))
+      GH_CHECK(pol.parse(e), H2H_ERR_ARG, "GPUH2H_TILE_POLICY: expected 8 entries small_work/col_block/sep_chunk");
+    FillPlan plan({&g}, pol);
+    GH_CUDA(cudaDeviceSynchronize());
+    g.t.translate_labels = clk.us();
+    clk.reset();
+    cudaEvent_t ev[2];
+    GH_CUDA(cudaEventCreate(&ev[0]));
+    GH_CUDA(cudaEventCreate(&ev[1]));
+    float ms = 0;
+    try {
+      plan.enqueue(0, nullptr, nullptr, ev);
+      plan.check_error();
+      GH_CUDA(cudaEventElapsedTime(&ms, ev[0], ev[1]));
+    } catch (...) {
+      cudaEventDestroy(ev[0]);
+      cudaEventDestroy(ev[1]);
+      throw;
+    }
+    cudaEventDestroy(ev[0]);
+    cudaEventDestroy(ev[1]);
+    g.t.fill_gpu = (long long)(ms * 1000.0f);
+    plan.attach(true);
+    return;
+  }
   D.release();
   D.n = n;
   // padded row offsets
@@ -314,78 +736,32 @@ void fill_labels_gpu(Graph &g) {
   D.dis_padded = drow[n];
   D.pos = g.pos_hash[n];
   const int nlev = (int)g.tree_hash.size() - 1;
-  // L4 runs as a dataflow over the tree; L3 (order-dependent, as shipped)
-  // keeps the level-synchronous kernel that applies the reference's order.
-  const bool flow = g.label_mode == H2H_LABEL_L4 && !std::getenv("GPUH2H_LEVEL_FILL");
-
   int64_t tmp_bytes = 0;
-  D.drow = dalloc<int64_t>(n + 1, D.bytes);
-  D.dis = dalloc<int>(D.dis_padded, D.bytes);
-  D.pos_hash = dalloc<int64_t>(n + 1, D.bytes);
-  D.pos_pos = dalloc<int>(D.pos, D.bytes);
-  D.pos_id = dalloc<int>(D.pos, D.bytes);
-  D.father = dalloc<int>(n, D.bytes);
-  D.depth = dalloc<int>(n, D.bytes);
-  D.err = dalloc<int>(1, D.bytes);
-  int *d_pos_w = dalloc<int>(D.pos, tmp_bytes);
-  int *d_nodes = dalloc<int>(n, tmp_bytes);
-  int *d_aux = dalloc<int>(n, tmp_bytes);          // level index (level path) or child count (flow path)
-  int *d_done = nullptr, *d_next = nullptr, *d_chainf = nullptr, *d_tiles = nullptr;
+  D.drow = dalloc_owned<int64_t>(n + 1, D);
+  D.dis = dalloc_owned<int>(D.dis_padded, D);
+  D.pos_hash = dalloc_owned<int64_t>(n + 1, D);
+  D.pos_pos = dalloc_owned<int>(D.pos, D);
+  D.pos_id = dalloc_owned<int>(D.pos, D);
+  D.father = dalloc_owned<int>(n, D);
+  D.depth = dalloc_owned<int>(n, D);
+  D.err = dalloc_owned<int>(1, D);
+  int *d_pos_w = nullptr, *d_nodes = nullptr, *d_aux = nullptr;
   int64_t *d_chain[2] = {nullptr, nullptr};
   auto cleanup = [&]() {
-    cudaFree(d_pos_w); cudaFree(d_nodes); cudaFree(d_aux); cudaFree(d_done); cudaFree(d_next); cudaFree(d_chainf);
-    cudaFree(d_tiles);
-    cudaFree(d_chain[0]); cudaFree(d_chain[1]);
+    cudaFree(d_pos_w); cudaFree(d_nodes); cudaFree(d_aux); cudaFree(d_chain[0]); cudaFree(d_chain[1]);
   };
   try {
+    d_pos_w = dalloc<int>(D.pos, tmp_bytes);
+    d_nodes = dalloc<int>(n, tmp_bytes);
+    d_aux = dalloc<int>(n, tmp_bytes);  // index of the node within its level
     std::vector<int> aux(n, 0);
     int64_t chain_max = 1;
-    // tiles of the dataflow fill: a node whose separator work m*d is small is
-    // one tile; a larger one is cut into column blocks x separator chunks so
-    // the thin, clique-heavy top of the tree spreads over many SMs
-    std::vector<int> tn, tc0, tc1, tu0, tu1, nt(n, 0);
-    int max_u = 1, max_c = 1;
-    if (flow) {
-      for (int v = 0; v < n; v++) aux[v] = g.child_off[v + 1] - g.child_off[v];
-      const int kSmallWork = 1 << 16, kColBlock = 128, kSepChunk = 32;
-      for (int i = 0; i < n; i++) {
-        const int v = g.tree_bfs[i], d = g.depth[v];
-        const int m = (int)(g.pos_hash[v + 1] - g.pos_hash[v]) - 1;
-        if ((int64_t)m * d <= kSmallWork && m <= 256) {
-          tn.push_back(v); tc0.push_back(0); tc1.push_back(d); tu0.push_back(0); tu1.push_back(m);
-          nt[v] = 1;
-          max_u = std::max(max_u, m);
-          max_c = std::max(max_c, d);
-        } else {
-          for (int c = 0; c < d; c += kColBlock)
-            for (int u = 0; u < std::max(m, 1); u += kSepChunk) {
-              tn.push_back(v); tc0.push_back(c); tc1.push_back(std::min(d, c + kColBlock));
-              tu0.push_back(u); tu1.push_back(std::min(m, u + kSepChunk));
-              nt[v]++;
-            }
-          max_u = std::max(max_u, std::min(m, kSepChunk));
-          max_c = std::max(max_c, kColBlock);
-        }
-      }
-      const int64_t ntiles = (int64_t)tn.size();
-      d_done = dalloc<int>(2 * (int64_t)n, tmp_bytes);     // done flags, then per-node tile counters
-      d_next = dalloc<int>(1, tmp_bytes);
-      d_chainf = dalloc<int>(D.dis_padded, tmp_bytes);
-      d_tiles = dalloc<int>(5 * ntiles + n, tmp_bytes);   // node, c0, c1, u0, u1, then tiles per node
-      GH_CUDA(cudaMemset(d_done, 0, sizeof(int) * 2 * (int64_t)n));
-      GH_CUDA(cudaMemset(d_next, 0, sizeof(int)));
-      const std::vector<int> *parts[5] = {&tn, &tc0, &tc1, &tu0, &tu1};
-      for (int k = 0; k < 5; k++)
-        GH_CUDA(cudaMemcpy(d_tiles + k * ntiles, parts[k]->data(), sizeof(int) * ntiles, cudaMemcpyHostToDevice));
-      GH_CUDA(cudaMemcpy(d_tiles + 5 * ntiles, nt.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
-    } else {
-      for (int l = 0; l < nlev; l++)
-        for (int i = g.tree_hash[l]; i < g.tree_hash[l + 1]; i++) aux[g.tree_bfs[i]] = i - g.tree_hash[l];
-      for (int l = 0; l < nlev; l++)
-        chain_max = std::max<int64_t>(chain_max, (int64_t)(g.tree_hash[l + 1] - g.tree_hash[l]) * l);
-      d_chain[0] = dalloc<int64_t>(chain_max, tmp_bytes);
-      d_chain[1] = dalloc<int64_t>(chain_max, tmp_bytes);
-    }
+    for (int l = 0; l < nlev; l++)
+      for (int i = g.tree_hash[l]; i < g.tree_hash[l + 1]; i++) aux[g.tree_bfs[i]] = i - g.tree_hash[l];
+    for (int l = 0; l < nlev; l++)
+      chain_max = std::max<int64_t>(chain_max, (int64_t)(g.tree_hash[l + 1] - g.tree_hash[l]) * l);
+    d_chain[0] = dalloc<int64_t>(chain_max, tmp_bytes);
+    d_chain[1] = dalloc<int64_t>(chain_max, tmp_bytes);
     GH_CUDA(cudaMemcpy(D.drow, drow.data(), sizeof(int64_t) * (n + 1), cudaMemcpyHostToDevice));
     GH_CUDA(cudaMemcpy(D.pos_hash, g.pos_hash.data(), sizeof(int64_t) * (n + 1), cudaMemcpyHostToDevice));
     GH_CUDA(cudaMemcpy(D.pos_pos, g.pos_pos.data(), sizeof(int) * D.pos, cudaMemcpyHostToDevice));
@@ -396,15 +772,9 @@ void fill_labels_gpu(Graph &g) {
     GH_CUDA(cudaMemcpy(d_nodes, g.tree_bfs.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
     GH_CUDA(cudaMemcpy(d_aux, aux.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
     GH_CUDA(cudaMemset(D.err, 0, sizeof(int)));
-    if (flow) {  // rows start at INT_MAX: split tiles combine with atomicMin; padding stays defined
-      fill_int_kernel<<<1024, 256>>>(D.dis, D.dis_padded, INT_MAX);
-      GH_CUDA(cudaGetLastError());
-    }
-    if (!flow) {
-      init_rows_kernel<<<std::max(1, std::min(65535, (n * 32 + 255) / 256)), 256>>>(D.drow, D.depth, D.pos_hash,
-                                                                                    D.pos_pos, d_pos_w, D.dis, n);
-      GH_CUDA(cudaGetLastError());
-    }
+    init_rows_kernel<<<std::max(1, std::min(65535, (n * 32 + 255) / 256)), 256>>>(D.drow, D.depth, D.pos_hash,
+                                                                                  D.pos_pos, d_pos_w, D.dis, n);
+    GH_CUDA(cudaGetLastError());
     GH_CUDA(cudaDeviceSynchronize());
     g.t.translate_labels = clk.us();
     clk.reset();
@@ -415,69 +785,30 @@ void fill_labels_gpu(Graph &g) {
     GH_CUDA(cudaEventCreate(&e0));
     GH_CUDA(cudaEventCreate(&e1));
     GH_CUDA(cudaEventRecord(e0));
-    if (flow) {
-      const int smem_dyn = enable_max_dynamic_smem(fill_flow_kernel);
-      const size_t smem = (size_t)max_u * 16 + (size_t)max_c * 8;
-      GH_CHECK(smem <= (size_t)smem_dyn, H2H_ERR_DEVICE, "separator or tree too large for the fill staging");
-      const int threads = 128;
-      int per_sm = 0;
-      GH_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fill_flow_kernel, threads, smem));
-      per_sm = std::max(1, per_sm);
-      const int64_t ntiles = (int64_t)tn.size();
-      FlowArgs A;
-      A.tile_node = d_tiles;
-      A.tile_c0 = d_tiles + ntiles;
-      A.tile_c1 = d_tiles + 2 * ntiles;
-      A.tile_u0 = d_tiles + 3 * ntiles;
-      A.tile_u1 = d_tiles + 4 * ntiles;
-      A.ntiles = (int)ntiles;
-      A.node_ntiles = d_tiles + 5 * ntiles;
-      A.node_cnt = d_done + n;
+    const int smem_dyn = enable_max_dynamic_smem(fill_level_kernel);
+    for (int l = 1; l < nlev; l++) {
+      const int d = l + 1;
+      const size_t per_warp = (size_t)((d + 3) & ~3) * 4 + (size_t)d * 8;
+      int wpb = (int)std::min<size_t>(8, (size_t)smem_dyn / per_warp);
+      GH_CHECK(wpb >= 1, H2H_ERR_DEVICE, "tree too deep for the shared-memory row staging");
+      const int count = g.tree_hash[l + 1] - g.tree_hash[l];
+      FillArgs A;
+      A.nodes = d_nodes + g.tree_hash[l];
+      A.count = count;
+      A.level = l;
       A.father = D.father;
-      A.depth = D.depth;
-      A.nchild = d_aux;
+      A.lvl_idx = d_aux;
       A.drow = D.drow;
       A.dis = D.dis;
       A.pos_hash = D.pos_hash;
       A.pos_id = D.pos_id;
       A.pos_pos = D.pos_pos;
-      A.pos_w = d_pos_w;
-      A.chain = d_chainf;
-      A.done = d_done;
-      A.next = d_next;
-      A.err = D.err;
-      A.spin_limit = spin_limit_cycles();
-      A.max_u = max_u;
-      A.max_c = max_c;
-      const int blocks = (int)std::min<int64_t>((int64_t)nsm * per_sm, ntiles);
-      fill_flow_kernel<<<std::max(1, blocks), threads, smem>>>(A);
+      A.chain_prev = d_chain[(l + 1) & 1];
+      A.chain_cur = (l + 1 < nlev) ? d_chain[l & 1] : nullptr;
+      A.l4 = g.label_mode == H2H_LABEL_L4;
+      int blocks = (int)std::min<int64_t>((count + wpb - 1) / wpb, (int64_t)nsm * 16);
+      fill_level_kernel<<<std::max(1, blocks), wpb * 32, per_warp * wpb>>>(A);
       GH_CUDA(cudaGetLastError());
-    } else {
-      const int smem_dyn = enable_max_dynamic_smem(fill_level_kernel);
-      for (int l = 1; l < nlev; l++) {
-        const int d = l + 1;
-        const size_t per_warp = (size_t)((d + 3) & ~3) * 4 + (size_t)d * 8;
-        int wpb = (int)std::min<size_t>(8, (size_t)smem_dyn / per_warp);
-        GH_CHECK(wpb >= 1, H2H_ERR_DEVICE, "tree too deep for the shared-memory row staging");
-        const int count = g.tree_hash[l + 1] - g.tree_hash[l];
-        FillArgs A;
-        A.nodes = d_nodes + g.tree_hash[l];
-        A.count = count;
-        A.level = l;
-        A.father = D.father;
-        A.lvl_idx = d_aux;
-        A.drow = D.drow;
-        A.dis = D.dis;
-        A.pos_hash = D.pos_hash;
-        A.pos_id = D.pos_id;
-        A.pos_pos = D.pos_pos;
-        A.chain_prev = d_chain[(l + 1) & 1];
-        A.chain_cur = (l + 1 < nlev) ? d_chain[l & 1] : nullptr;
-        A.l4 = g.label_mode == H2H_LABEL_L4;
-        int blocks = (int)std::min<int64_t>((count + wpb - 1) / wpb, (int64_t)nsm * 16);
-        fill_level_kernel<<<std::max(1, blocks), wpb * 32, per_warp * wpb>>>(A);
-        GH_CUDA(cudaGetLastError());
-      }
     }
     GH_CUDA(cudaEventRecord(e1));
     GH_CUDA(cudaEventSynchronize(e1));
@@ -486,9 +817,6 @@ void fill_labels_gpu(Graph &g) {
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     g.t.fill_gpu = (long long)(ms * 1000.0f);
-    int kerr = 0;
-    GH_CUDA(cudaMemcpy(&kerr, D.err, sizeof(int), cudaMemcpyDeviceToHost));
-    GH_CHECK(kerr == 0, H2H_ERR_DEVICE, "label fill: a dependency wait ran out (error code " + std::to_string(kerr) + ")");
     max_label_kernel<<<nsm * 4, 256>>>(D.dis, D.dis_padded, D.err);
     GH_CUDA(cudaGetLastError());
     int mx = 0;
@@ -504,12 +832,17 @@ void fill_labels_gpu(Graph &g) {
 }
 
 // Copies the filled labels back into the reference's unpadded layout.
+// The graph's rows are [drow_host[0], drow_host[n]) of the device array
+// (a batch's forest array holds other graphs' rows around them).
 void download_labels(const Graph &g, int *dis_out) {
   const int n = g.n;
-  std::vector<int> tmp(g.dev.dis_padded);
-  GH_CUDA(cudaMemcpy(tmp.data(), g.dev.dis, sizeof(int) * g.dev.dis_padded, cudaMemcpyDeviceToHost));
+  const int64_t r0 = g.drow_host[0], r1 = g.drow_host[n];
+  GH_CHECK(r1 - r0 == g.dev.dis_padded, H2H_ERR_STATE, "label rows and device index disagree");
+  std::vector<int> tmp(r1 - r0);
+  GH_CUDA(cudaMemcpy(tmp.data(), g.dev.dis + r0, sizeof(int) * (r1 - r0), cudaMemcpyDeviceToHost));
   for (int v = 0; v < n; v++)
-    std::copy(tmp.begin() + g.drow_host[v], tmp.begin() + g.drow_host[v] + g.depth[v], dis_out + g.dis_hash[v]);
+    std::copy(tmp.begin() + (g.drow_host[v] - r0), tmp.begin() + (g.drow_host[v] - r0) + g.depth[v],
+              dis_out + g.dis_hash[v]);
 }
 
 }  // namespace gh

@@ -165,8 +165,11 @@ void upload_query_index(Graph &g) {
   D.euler = g.euler_n;
   D.rmq = (int64_t)g.rmq_id.size();
   D.first = dalloc<int>(n, D.bytes);
+  D.owned.push_back(D.first);
   D.rmq_hash = dalloc<int64_t>(D.euler, D.bytes);
+  D.owned.push_back(D.rmq_hash);
   D.rmq_id = dalloc<int>(D.rmq, D.bytes);
+  D.owned.push_back(D.rmq_id);
   GH_CUDA(cudaMemcpy(D.first, g.first.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
   GH_CUDA(cudaMemcpy(D.rmq_hash, g.rmq_hash.data(), sizeof(int64_t) * D.euler, cudaMemcpyHostToDevice));
   GH_CUDA(cudaMemcpy(D.rmq_id, g.rmq_id.data(), sizeof(int) * D.rmq, cudaMemcpyHostToDevice));

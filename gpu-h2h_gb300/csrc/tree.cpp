@@ -117,10 +117,16 @@ void allocate_labels_and_bfs(Graph &g) {
   g.pos_id.resize(g.pos_hash[n]);
   g.pos_pos.resize(g.pos_hash[n]);
   g.pos_w.resize(g.pos_hash[n]);
+  g.pos_src.resize(g.pos_hash[n]);
   Pool pool(g.threads);
   std::atomic<int> bad{-1};
   pool.parallel_for(n, 1024, [&](int64_t b, int64_t e, int) {
-    std::vector<std::pair<int64_t, int>> tmp;
+    struct Entry {
+      int64_t key;  // position << 32 | id
+      int w, src;
+      bool operator<(const Entry &o) const { return key < o.key; }
+    };
+    std::vector<Entry> tmp;
     for (int64_t vv = b; vv < e; vv++) {
       const int v = (int)vv;
       const int d = g.depth[v];
@@ -128,15 +134,16 @@ void allocate_labels_and_bfs(Graph &g) {
       for (int64_t k = g.x_off[v]; k < g.x_off[v + 1]; k++) {
         int a = g.x_id[k], p = g.depth[a] - 1;
         if (p < 0 || p >= d - 1) { bad = v; continue; }
-        tmp.push_back({(int64_t)p << 32 | (uint32_t)a, g.x_w[k]});
+        tmp.push_back({(int64_t)p << 32 | (uint32_t)a, g.x_w[k], (int)(k - g.x_off[v])});
       }
-      tmp.push_back({(int64_t)(d - 1) << 32 | (uint32_t)v, 0});
+      tmp.push_back({(int64_t)(d - 1) << 32 | (uint32_t)v, 0, -1});
       std::sort(tmp.begin(), tmp.end());  // positions are distinct
       int64_t o = g.pos_hash[v];
       for (size_t k = 0; k < tmp.size(); k++) {
-        g.pos_pos[o + k] = (int)(tmp[k].first >> 32);
-        g.pos_id[o + k] = (int)(tmp[k].first & 0xffffffff);
-        g.pos_w[o + k] = tmp[k].second;
+        g.pos_pos[o + k] = (int)(tmp[k].key >> 32);
+        g.pos_id[o + k] = (int)(tmp[k].key & 0xffffffff);
+        g.pos_w[o + k] = tmp[k].w;
+        g.pos_src[o + k] = tmp[k].src;
       }
     }
   });

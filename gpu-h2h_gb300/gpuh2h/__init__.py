@@ -40,6 +40,14 @@ class _Info(C.Structure):
                                           "max_label", "label_updates")]
 
 
+class _BatchInfo(C.Structure):
+    _fields_ = [(f, C.c_int32) for f in ("graphs", "vertices", "elim_launches", "graph_captured")] + \
+               [(f, C.c_int64) for f in ("fill_tiles", "device_bytes", "label_updates", "t_sets_us", "t_plan_us",
+                                          "t_contract_us", "t_global_us", "t_download_us", "t_tree_us",
+                                          "t_fill_plan_us", "t_fill_us", "t_attach_us", "t_total_us",
+                                          "t_rebuild_us", "t_rebuild_fill_us")]
+
+
 class GenParams(C.Structure):
     _fields_ = [("n", C.c_int64), ("cols", C.c_int32), ("aspect_milli", C.c_int32), ("jitter_milli", C.c_int32),
                 ("drop_permille", C.c_int32), ("target_arcs", C.c_int64), ("diag_permille", C.c_int32),
@@ -79,6 +87,16 @@ SIGNATURES = {
     "h2h_gen_local_pairs": (_i32, [_vp, _i64, _i32, C.c_uint64, _vp, _vp]),
     "h2h_fill_labels_l4_noalloc": (_i32, [_i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i64, _vp, _i32, _i32,
                                           _vp]),
+    "h2h_copy_input_arcs": (_i32, [_vp, _vp, _vp, _vp]),
+    "h2h_batch_build": (_i32, [_vp, _i32, _i32, C.POINTER(_vp)]),
+    "h2h_batch_set_weights": (_i32, [_vp, _i32, _vp]),
+    "h2h_batch_rebuild": (_i32, [_vp]),
+    "h2h_batch_sync_host": (_i32, [_vp]),
+    "h2h_batch_set_policy": (_i32, [_vp, _cp]),
+    "h2h_batch_get_policy": (_i32, [_vp, _vp, _i32]),
+    "h2h_batch_tune": (_i32, [_vp, _i32, _vp, _i32]),
+    "h2h_batch_get_info": (_i32, [_vp, C.POINTER(_BatchInfo)]),
+    "h2h_batch_free": (None, [_vp]),
 }
 
 _lib = None
@@ -275,6 +293,15 @@ class Graph:
         _check(self._L.h2h_copy_bfs(self.h, _p(tb), _p(th)))
         return tb, th
 
+    def input_arcs(self):
+        """Stored arcs in CSR order (the order h2h_batch_set_weights takes)."""
+        i = self.info()
+        off = np.empty(i["n"] + 1, np.int32)
+        v = np.empty(i["m"], np.int32)
+        w = np.empty(i["m"], np.int32)
+        _check(self._L.h2h_copy_input_arcs(self.h, _p(off), _p(v), _p(w)))
+        return off, v, w
+
     def local_pairs(self, n: int, max_hops: int = 20, seed: int = 1):
         x = np.empty(n, np.int32)
         y = np.empty(n, np.int32)
@@ -297,6 +324,64 @@ class Graph:
         _check(self._L.h2h_write_query_result(self.h, root.encode(), query_number, _p(t)))
 
 
+class Batch:
+    """Several loaded graphs contracted and labelled together (h2h_batch_*).
+
+    Batch(graphs, threads) builds every graph; afterwards each Graph answers
+    queries on its own.  The Graph objects must stay open while the batch
+    lives (the batch keeps references to them).
+    """
+
+    def __init__(self, graphs, threads: int = 8):
+        _require_gpu()
+        L = load_library()
+        self._L = L
+        self.graphs = list(graphs)
+        arr = (C.c_void_p * len(self.graphs))(*[g.h for g in self.graphs])
+        b = C.c_void_p()
+        _check(L.h2h_batch_build(C.cast(arr, C.c_void_p), len(self.graphs), threads, C.byref(b)))
+        self.b = b
+
+    def close(self):
+        if getattr(self, "b", None):
+            self._L.h2h_batch_free(self.b)
+            self.b = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def info(self) -> dict:
+        inf = _BatchInfo()
+        _check(self._L.h2h_batch_get_info(self.b, C.byref(inf)))
+        return {f: getattr(inf, f) for f, _ in _BatchInfo._fields_}
+
+    def set_weights(self, index: int, w: np.ndarray):
+        w = np.ascontiguousarray(w, np.int32)
+        _check(self._L.h2h_batch_set_weights(self.b, index, _p(w)))
+
+    def rebuild(self):
+        _check(self._L.h2h_batch_rebuild(self.b))
+
+    def sync_host(self):
+        _check(self._L.h2h_batch_sync_host(self.b))
+
+    def policy(self) -> str:
+        buf = C.create_string_buffer(512)
+        _check(self._L.h2h_batch_get_policy(self.b, C.cast(buf, C.c_void_p), 512))
+        return buf.value.decode()
+
+    def set_policy(self, policy: str):
+        _check(self._L.h2h_batch_set_policy(self.b, policy.encode()))
+
+    def tune(self, rounds: int = 1) -> str:
+        buf = C.create_string_buffer(512)
+        _check(self._L.h2h_batch_tune(self.b, rounds, C.cast(buf, C.c_void_p), 512))
+        return buf.value.decode()
+
+
 def gen_params(**kw) -> GenParams:
     p = GenParams()
     load_library().h2h_gen_default(C.byref(p))
@@ -311,6 +396,33 @@ def generate_road(root: str, name: str, **kw) -> int:
     arcs = C.c_int64()
     _check(load_library().h2h_generate_road(C.byref(p), root.encode(), name.encode(), C.byref(arcs)))
     return arcs.value
+
+
+def road_batch_params(count: int = 64, n_lo: int = 2000, n_hi: int = 200000, seed: int = 7) -> list:
+    """Generator parameters of `count` road graphs with vertex counts drawn
+    log-uniform in [n_lo, n_hi] (seeded), the 264,346-vertex road graph's
+    shape (jittered 1:1.3 grid, 2.776 arcs per vertex, 0.5% highway layer),
+    partition height ceil(log2(n / 256)) (at least 2)."""
+    import math
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(count):
+        n = int(round(math.exp(rng.uniform(math.log(n_lo), math.log(n_hi)))))
+        out.append(dict(n=n, target_arcs=int(round(n * 733846 / 264346)), aspect_milli=1300, jitter_milli=300,
+                        diag_permille=50, hw_tiers=1, hw_permille10=50, hw_k=3, hw_scale_milli=400,
+                        partition_height=max(2, math.ceil(math.log2(n / 256))), seed=1000 + i, cols=0,
+                        drop_permille=0))
+    return out
+
+
+def write_edge_file(path: str, off: np.ndarray, v: np.ndarray, w: np.ndarray):
+    """An Edge file (1-based `a u v w` lines) holding the stored arcs in CSR
+    order, so a graph loaded from it has exactly these arcs."""
+    n = len(off) - 1
+    src = np.repeat(np.arange(n, dtype=np.int64), np.diff(off.astype(np.int64)))
+    with open(path, "w") as f:
+        f.write("%d %d\n" % (n, len(v)))
+        f.write("".join("a %d %d %d\n" % (a + 1, b + 1, c) for a, b, c in zip(src, v, w)))
 
 
 def uniform_pairs(n_vertices: int, n: int, seed: int = 1):

@@ -157,6 +157,56 @@ int h2h_fill_labels_l4_noalloc(int n, const int *order, const int *father, const
                                const int64_t *dis_hash, int64_t total_label, int *dis, int max_depth, int max_sep,
                                void *stream);
 
+/* ---- Batched construction.  No counterpart in the reference, which builds
+ * one graph per process (main.cu:84-147).  Many loaded graphs are contracted
+ * together (one elimination launch per level step across every graph, one
+ * launch for every graph's global order over levels <= C) and labelled (L4)
+ * by one dataflow launch over the forest of their trees.  Each graph ends in
+ * the state h2h_contract(g, 1) + h2h_build_labels(g, 2, 1, H2H_LABEL_L4)
+ * leaves, with bit-identical order, tree and labels, and answers queries on
+ * its own handle.  The graphs must outlive the batch. */
+typedef struct h2h_batch h2h_batch;
+
+typedef struct {
+  int32_t graphs, vertices, elim_launches, graph_captured;
+  int64_t fill_tiles, device_bytes, label_updates;
+  int64_t t_sets_us, t_plan_us, t_contract_us, t_global_us, t_download_us, t_tree_us, t_fill_plan_us, t_fill_us,
+      t_attach_us, t_total_us; /* the batched build, by phase (wall time; GPU phases by CUDA events) */
+  int64_t t_rebuild_us;       /* device time of the last h2h_batch_rebuild */
+  int64_t t_rebuild_fill_us;  /* its label-fill part */
+} h2h_batch_info;
+
+/* Builds `count` graphs loaded by h2h_load / h2h_load_files and not yet
+ * contracted.  threads: host threads for the per-graph host phases (each
+ * graph's own phase runs on one thread). */
+int h2h_batch_build(h2h_graph *const *graphs, int count, int threads, h2h_batch **out);
+/* Replaces the arc weights of graph `index` for the next h2h_batch_rebuild:
+ * w holds one weight per stored arc in h2h_copy_input_arcs order. */
+int h2h_batch_set_weights(h2h_batch *b, int index, const int *w);
+/* Recomputes contraction and labels of every graph from the current weights
+ * on the GPU, replaying one CUDA graph captured on the first call (the tree
+ * shape depends only on the arcs, not on their weights, so it is kept).
+ * Waits for the result; the graphs' queries see the new labels. */
+int h2h_batch_rebuild(h2h_batch *b);
+/* Brings the host copies of the shortcut weights (h2h_copy_adj) in line
+ * with the last rebuild. */
+int h2h_batch_sync_host(h2h_batch *b);
+/* Tile shapes of the forest label fill.  policy is 8 entries
+ * "small_work/col_block/sep_chunk" separated by spaces: level width below /
+ * at least the SM count, times separator size m <= 16, <= 64, <= 256, > 256.
+ * h2h_batch_tune times candidate shapes on this batch (coordinate descent,
+ * `rounds` passes), keeps the fastest and writes it to policy_out. */
+int h2h_batch_set_policy(h2h_batch *b, const char *policy);
+int h2h_batch_get_policy(const h2h_batch *b, char *policy_out, int cap);
+int h2h_batch_tune(h2h_batch *b, int rounds, char *policy_out, int cap);
+int h2h_batch_get_info(const h2h_batch *b, h2h_batch_info *info);
+void h2h_batch_free(h2h_batch *b);
+
+/* The stored arcs of a loaded graph in CSR order (self-loops dropped,
+ * parallel arcs kept, each vertex's arcs in Edge-file order):
+ * adj_off[n+1], adj_v[m], adj_w[m]. */
+int h2h_copy_input_arcs(const h2h_graph *g, int *adj_off, int *adj_v, int *adj_w);
+
 #ifdef __cplusplus
 }
 #endif
