@@ -21,6 +21,7 @@ from __future__ import annotations
 import argparse
 import json
 import os
+import shutil
 import statistics
 import subprocess
 import sys
@@ -51,6 +52,77 @@ def gen_graph(root: str):
     kw.update(cols=0, drop_permille=0)
     arcs = gpuh2h.generate_road(root, WORKLOAD["name"], **kw)
     return gpuh2h.files_for(root, WORKLOAD["name"]), arcs
+
+
+def batched_build(threads: int, count: int) -> dict:
+    """64 road graphs (log-uniform 2,000-200,000 vertices, partition height
+    ceil(log2(n/256)), C = 2), built once as sequential single-graph builds
+    (h2h_contract + h2h_build_labels per graph) and once as one batch
+    (h2h_batch_build), then rebuilt from the device state after a weight
+    update (h2h_batch_rebuild: one CUDA graph replay) with the default and the
+    autotuned fill tile shapes.  Parity: every graph's answers to 10^4 seeded
+    pairs, max label and label count equal its sequential build's."""
+    import torch
+
+    import gpuh2h
+    root = tempfile.mkdtemp(prefix="h2h_batch_")
+    params = gpuh2h.road_batch_params(count, 2000, 200000, seed=7)
+    specs = []
+    for i, p in enumerate(params):
+        name = "g%02d" % i
+        gpuh2h.generate_road(root, name, **p)
+        specs.append((gpuh2h.files_for(root, name), p["partition_height"]))
+    load = lambda: [gpuh2h.Graph("g", H, 2, threads, 1, files=f) for f, H in specs]
+    seq = load()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for g in seq:
+        g.contraction_noHub(1)
+        g.constructLabel_noHub(2, 1, gpuh2h.LABEL_L4)
+    seq_s = time.perf_counter() - t0
+    bat = load()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    b = gpuh2h.Batch(bat, threads)
+    batch_s = time.perf_counter() - t0
+    cold = b.info()
+
+    def check():
+        for i, (gs, gb) in enumerate(zip(seq, bat)):
+            n = gs.info()["n"]
+            x, y = gpuh2h.uniform_pairs(n, 10_000, 100 + i)
+            assert np.array_equal(gs.query(x, y), gb.query(x, y)), "batch graph %d answers differ" % i
+            a, c = gs.info(), gb.info()
+            assert a["max_label"] == c["max_label"] and a["label_size"] == c["label_size"]
+    check()
+
+    def rebuilds(k=5):
+        ts = []
+        for _ in range(k):
+            b.rebuild()
+            ts.append(b.info()["t_rebuild_us"] / 1e6)
+        return statistics.median(ts)
+    b.rebuild()  # first call captures the CUDA graph
+    reb_default = rebuilds()
+    t0 = time.perf_counter()
+    policy = b.tune(1)
+    tune_s = time.perf_counter() - t0
+    reb_tuned = rebuilds()
+    check()
+    nv = sum(gs.info()["n"] for gs in seq)
+    out = {"graphs": count, "vertices": nv, "label_entries": sum(gs.info()["label_size"] for gs in seq),
+           "sequential_s": seq_s, "batched_s": batch_s, "speedup_cold": seq_s / batch_s,
+           "batched_phases_ms": {k[2:-3]: cold[k] / 1e3 for k in cold if k.startswith("t_") and k.endswith("_us")
+                                 and not k.startswith("t_rebuild")},
+           "elim_launches": cold["elim_launches"], "fill_tiles": cold["fill_tiles"],
+           "rebuild_s_default_tiles": reb_default, "rebuild_s_tuned_tiles": reb_tuned,
+           "speedup_rebuild_vs_sequential": seq_s / reb_tuned, "tuned_policy": policy, "tune_s": tune_s,
+           "parity": "answers to 1e4 pairs per graph, max label and label count equal the sequential builds'"}
+    b.close()
+    for g in seq + bat:
+        g.close()
+    shutil.rmtree(root, ignore_errors=True)
+    return out
 
 
 def query_pairs(g, n_vertices: int, seed: int):
@@ -252,6 +324,7 @@ def main():
     ap.add_argument("--latency-batches", type=int, default=200)
     ap.add_argument("--cpu-budget", type=float, default=10.0, help="seconds of CPU query work for cpu_baseline")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--batch-graphs", type=int, default=64, help="graphs of the batched-build measurement (0: skip)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -377,6 +450,10 @@ def main():
         g.query_host_ptr(xh.data_ptr() + 4 * off, yh.data_ptr() + 4 * off, oh.data_ptr() + 4 * off, bq,
                          gpuh2h.QUERY_LCA)
         lat_e2e.append((time.perf_counter() - s) * 1e6)
+    # ---- batched construction of many graphs (rank 0, N=1 only)
+    batched = None
+    if rank == 0 and world == 1 and args.batch_graphs > 0:
+        batched = batched_build(threads, args.batch_graphs)
     # ---- CPU baseline (rank 0, N=1 only): the reference's CPU algorithm on host cores
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -419,6 +496,7 @@ def main():
                      "traffic": traffic, "peak_source": peak_src, "algorithmic_bytes_per_launch": abytes,
                      "kernel": "query_tile_kernel<LCA>"},
         "clocks": clocks,
+        "batched_build": batched,
         "cpu_baseline": cpu,
     }
     if rank == 0:

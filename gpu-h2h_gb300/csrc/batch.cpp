@@ -16,6 +16,8 @@
 // elimination launch, the gather of shortcut weights into the pos entries
 // and the fill, captured once as a CUDA graph.
 #include <algorithm>
+#include <cstdlib>
+#include <cstdio>
 #include <cstring>
 #include <memory>
 
@@ -103,7 +105,10 @@ int h2h_batch_build(h2h_graph *const *graphs, int count, int threads, h2h_batch 
     }
     gh::Clock total, clk;
     gh::Pool pool(std::max(1, threads));
-    // per-graph host phases run one graph per thread
+    // per-graph host phases run one graph per thread, largest graph first
+    std::vector<int> by_size(count);
+    for (int i = 0; i < count; i++) by_size[i] = i;
+    std::stable_sort(by_size.begin(), by_size.end(), [&](int x, int y) { return b->gs[x]->m > b->gs[y]->m; });
     auto per_graph = [&](const std::function<void(gh::Graph &)> &fn) {
       std::vector<int> saved(count);
       for (int i = 0; i < count; i++) {
@@ -112,7 +117,8 @@ int h2h_batch_build(h2h_graph *const *graphs, int count, int threads, h2h_batch 
       }
       std::vector<std::exception_ptr> errs(count);
       pool.parallel_for(count, 1, [&](int64_t lo, int64_t hi, int) {
-        for (int64_t i = lo; i < hi; i++) {
+        for (int64_t k = lo; k < hi; k++) {
+          const int i = by_size[k];
           try {
             fn(*b->gs[i]);
           } catch (...) {
@@ -135,7 +141,7 @@ int h2h_batch_build(h2h_graph *const *graphs, int count, int threads, h2h_batch 
     clk.reset();
     GH_CUDA(cudaEventRecord(b->ev[0], b->stream));
     cudaEvent_t hev[2] = {b->ev[1], b->ev[2]};
-    b->elim->enqueue(b->stream, hev);
+    b->elim->enqueue(b->stream, hev, std::getenv("GPUH2H_TRACE") != nullptr);
     b->elim->check_error();
     b->info.t_contract_us = event_us(b->ev[0], b->ev[1]);
     b->info.t_global_us = event_us(b->ev[1], b->ev[2]);
@@ -149,14 +155,25 @@ int h2h_batch_build(h2h_graph *const *graphs, int count, int threads, h2h_batch 
     b->info.t_download_us = clk.us();
     clk.reset();
     per_graph([](gh::Graph &g) {
-      gh::build_tree_and_rmq(g);
+      gh::build_tree(g);
       g.contracted = true;
       g.parallel_fine = 2;
       g.construct_device = 1;
       g.label_mode = H2H_LABEL_L4;
       gh::allocate_labels_and_bfs(g);
     });
+    gh::build_rmq_gpu(b->gs);
     b->info.t_tree_us = clk.us();
+    if (std::getenv("GPUH2H_TRACE")) {
+      long long sum = 0, mx = 0;
+      for (gh::Graph *g : b->gs) {
+        const long long t = g->t.tree + g->t.malloc_labels + g->t.bfs;
+        sum += t;
+        mx = std::max(mx, t);
+      }
+      std::fprintf(stderr, "[gpuh2h] batch tree phase: %lld us wall, per-graph sum %lld us, max %lld us\n",
+                   (long long)b->info.t_tree_us, sum, mx);
+    }
     clk.reset();
     gh::TilePolicy pol;
     if (const char *e = std::getenv("GPUH2H_TILE_POLICY"))

@@ -245,14 +245,14 @@ int h2h_get_info(const h2h_graph *h, h2h_info *info) {
   info->m = g.m;
   info->label_size = g.h2h_size;
   info->pos_size = g.pos_hash.empty() ? 0 : g.pos_hash.back();
-  info->rmq_size = (int64_t)g.rmq_id.size();
+  info->rmq_size = g.rmq_total;
   info->euler_size = g.euler_n;
   info->lub_size = g.lub;
   info->adj_size = g.x_off.empty() ? 0 : g.x_off.back();
   info->device_bytes = g.dev.bytes;
   info->lub_mb = (double)g.lub * 12.0 / MB;
   info->decomposition_tree_mb = (double)g.decomposition_size * 12.0 / MB;
-  info->rmq_mb = ((double)g.rmq_hash.size() * 8 + (double)g.rmq_id.size() * 4 + (double)g.n * 4) / MB;
+  info->rmq_mb = ((double)g.euler_n * 8 + (double)g.rmq_total * 4 + (double)g.n * 4) / MB;
   info->label_mb = ((double)(g.n + 1) * 16 + (double)info->pos_size * 4 + (double)g.h2h_size * 4) / MB;
   const gh::Timings &t = g.t;
   info->t_load_us = t.load;
@@ -299,8 +299,7 @@ int h2h_copy_rmq(const h2h_graph *h, int64_t *rmq_hash, int *rmq_id) {
   return guarded([&] {
     const gh::Graph &g = h->g;
     GH_CHECK(g.contracted, H2H_ERR_STATE, "not contracted");
-    if (rmq_hash) std::copy(g.rmq_hash.begin(), g.rmq_hash.end(), rmq_hash);
-    if (rmq_id) std::copy(g.rmq_id.begin(), g.rmq_id.end(), rmq_id);
+    gh::download_rmq(g, rmq_hash, rmq_id);
   });
 }
 

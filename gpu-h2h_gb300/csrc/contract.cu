@@ -44,11 +44,14 @@
 
 #include <algorithm>
 #include <climits>
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <exception>
 
 #include "graph.h"
+#include "pool.h"
 
 namespace cg = cooperative_groups;
 
@@ -561,13 +564,36 @@ ElimPlan::ElimPlan(const std::vector<Graph *> &graphs) : gs(graphs) {
   GH_CHECK(K >= 1, H2H_ERR_ARG, "no graph to contract");
   const bool force_global_stage = std::getenv("GPUH2H_GLOBAL_STAGING") != nullptr;
   std::vector<GraphLevels> L(K);
+  std::vector<std::vector<int>> bound(K);  // list bound per partition cell (levels > C)
+  int threads = 1;
+  for (const Graph *g : gs) threads = std::max(threads, g->threads);
+  {
+    Pool pool(std::min(threads, K));
+    std::vector<std::exception_ptr> errs(K);
+    pool.parallel_for(K, 1, [&](int64_t lo, int64_t hi, int) {
+      for (int64_t i = lo; i < hi; i++) {
+        try {
+          const Graph &g = *gs[i];
+          L[i] = graph_levels(g);
+          bound[i].assign(g.cell_start.size(), 1);
+          for (int h = g.H; h > g.C; h--) {
+            const int64_t clo = (int64_t(1) << (h - 1)) - 1, chi = (int64_t(1) << h) - 2;
+            for (int64_t c = clo; c <= chi; c++) bound[i][c] = cell_list_bound(g, L[i], c, h);
+          }
+        } catch (...) {
+          errs[i] = std::current_exception();
+        }
+      }
+    });
+    for (auto &e : errs)
+      if (e) std::rethrow_exception(e);
+  }
   std::vector<int64_t> lbase(K);
   vbase.assign(K, 0);
   mbase.assign(K, 0);
   int64_t pool_extra = 1024;
   for (int i = 0; i < K; i++) {
     Graph &g = *gs[i];
-    L[i] = graph_levels(g);
     vbase[i] = N;
     mbase[i] = M;
     lbase[i] = lub;
@@ -579,114 +605,173 @@ ElimPlan::ElimPlan(const std::vector<Graph *> &graphs) : gs(graphs) {
     pool_extra += (int64_t)L[i].heap_n * std::min(L[i].heap_n, 8192);
     g.gpu_vertices = L[i].heap_start;
   }
+  GH_CHECK(M < INT32_MAX, H2H_ERR_ARG, "too many arcs in one batch");
   // slot arrays: the LUB ranges, then a pool for global-order lists that
   // outgrow theirs
   pool_size = lub + pool_extra;
   // ---- forest arrays
   std::vector<int64_t> f_slot_off(N);
   std::vector<int> f_deg(N), f_cap(N), f_elim(N), f_adj_off(N + 1), f_adj_v(std::max<int64_t>(M, 1)),
-      f_adj_w(std::max<int64_t>(M, 1)), f_heap;
-  f_heap.reserve(heap_total);
-  for (int i = 0; i < K; i++) {
-    const Graph &g = *gs[i];
-    const int vb = vbase[i];
-    for (int v = 0; v < g.n; v++) {
-      f_slot_off[vb + v] = g.slot_off[v] + lbase[i];
-      f_deg[vb + v] = g.adj_off[v + 1] - g.adj_off[v];
-      f_cap[vb + v] = g.cap[v];
-      f_elim[vb + v] = g.elim[v] + vb;
-      f_adj_off[vb + v] = g.adj_off[v] + (int)mbase[i];
-    }
-    for (int64_t e = 0; e < g.m; e++) {
-      f_adj_v[mbase[i] + e] = g.adj_v[e] + vb;
-      f_adj_w[mbase[i] + e] = g.adj_w[e];
-    }
-    for (int j = L[i].heap_start; j < g.n; j++) f_heap.push_back(g.elim[j] + vb);
-  }
-  GH_CHECK(M < INT32_MAX, H2H_ERR_ARG, "too many arcs in one batch");
-  f_adj_off[N] = (int)M;
-  // ---- launches: step s takes level H_i - s of every graph still above C_i
-  std::vector<int> fcs, fcc;
-  int steps = 0;
-  for (int i = 0; i < K; i++) steps = std::max(steps, gs[i]->H - gs[i]->C);
-  struct Pending { int level; int64_t lo; int ncell, kmax, lmax; bool heap; };
-  std::vector<Pending> pend;
-  for (int st = 0; st < steps; st++) {
-    Pending P{0, (int64_t)fcs.size(), 0, 1, 1, false};
-    for (int i = 0; i < K; i++) {
-      const Graph &g = *gs[i];
-      const int h = g.H - st;
-      if (h <= g.C) continue;
-      P.level = h;
-      const int64_t lo = (int64_t(1) << (h - 1)) - 1, hi = (int64_t(1) << h) - 2;
-      for (int64_t c = lo; c <= hi; c++) {
-        fcs.push_back(vbase[i] + g.cell_start[c]);
-        fcc.push_back(g.cell_count[c]);
-        P.kmax = std::max(P.kmax, g.cell_count[c]);
-        P.lmax = std::max(P.lmax, cell_list_bound(g, L[i], c, h));
-      }
-    }
-    P.ncell = (int)(fcs.size() - P.lo);
-    if (K > 1) P.level = -(st + 1);  // a step, not one graph's level
-    if (P.ncell) pend.push_back(P);
-  }
+      f_adj_w(std::max<int64_t>(M, 1)), f_heap(std::max(heap_total, 1));
   {
-    Pending P{0, (int64_t)fcs.size(), K, 1, 1, true};
-    for (int i = 0; i < K; i++) {
-      fcs.push_back(vbase[i] + L[i].heap_start);
-      fcc.push_back(L[i].heap_n);
-      P.kmax = std::max(P.kmax, L[i].heap_n);
-      P.lmax = std::max(P.lmax, L[i].heap_n - 1);
-    }
-    pend.push_back(P);
+    std::vector<int> hbase(K, 0);
+    for (int i = 1; i < K; i++) hbase[i] = hbase[i - 1] + L[i - 1].heap_n;
+    Pool pool(std::min(threads, K));
+    pool.parallel_for(K, 1, [&](int64_t lo, int64_t hi, int) {
+      for (int64_t i = lo; i < hi; i++) {
+        const Graph &g = *gs[i];
+        const int vb = vbase[i];
+        for (int v = 0; v < g.n; v++) {
+          f_slot_off[vb + v] = g.slot_off[v] + lbase[i];
+          f_deg[vb + v] = g.adj_off[v + 1] - g.adj_off[v];
+          f_cap[vb + v] = g.cap[v];
+          f_elim[vb + v] = g.elim[v] + vb;
+          f_adj_off[vb + v] = g.adj_off[v] + (int)mbase[i];
+        }
+        for (int64_t e = 0; e < g.m; e++) {
+          f_adj_v[mbase[i] + e] = g.adj_v[e] + vb;
+          f_adj_w[mbase[i] + e] = g.adj_w[e];
+        }
+        for (int j = L[i].heap_start; j < g.n; j++) f_heap[hbase[i] + j - L[i].heap_start] = g.elim[j] + vb;
+      }
+    });
   }
-  // ---- launch shapes
+  f_adj_off[N] = (int)M;
+  // ---- launches.  Step s takes level H_i - s of every graph still above
+  // C_i; the last step takes every graph's global order as one cell per
+  // graph.  Within a step, cells are grouped by size class, each group is a
+  // launch with its own cluster size (a large cell spreads its merges over up
+  // to 16 CTAs), and the groups of a step run side by side on forked streams.
   const int smem_dyn = enable_max_dynamic_smem(elim_kernel);
   GH_CUDA(cudaFuncSetAttribute(elim_kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
   int dev = 0;
   GH_CUDA(cudaGetDevice(&dev));
   GH_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-  auto al = [](int64_t b) { return (b + 15) & ~int64_t(15); };
-  int64_t pstage_ints = 0;
-  for (const Pending &P : pend) {
-    Launch Lc;
-    Lc.level = P.level; Lc.lo = P.lo; Lc.ncell = P.ncell; Lc.kmax = P.kmax; Lc.lmax = P.lmax; Lc.heap = P.heap;
-    const int64_t keys_b = 3 * al(4LL * P.kmax);
-    const int64_t own_b = keys_b + 2 * al(4LL * P.lmax);
-    auto smem_for = [&](int w) { return own_b + 2 * al(4LL * P.lmax * w); };
-    int nw = P.ncell * 4 < nsm ? 16 : 8;
-    while (nw > 4 && smem_for(nw) > smem_dyn) nw >>= 1;
-    // per-warp merge buffers move to global memory when they do not fit
-    Lc.global_stage = smem_for(nw) > smem_dyn || force_global_stage;
-    if (Lc.global_stage) nw = P.ncell * 4 < nsm ? 16 : 8;
-    GH_CHECK(own_b <= smem_dyn, H2H_ERR_DEVICE,
-             "elimination staging does not fit shared memory (candidate keys + eliminated list too large)");
-    Lc.smem = Lc.global_stage ? own_b : smem_for(nw);
-    Lc.nw = nw;
-    // clusters: spread the few large cells of the top levels over many SMs
-    int cs = 1;
-    while (cs < 16 && (int64_t)P.ncell * cs * 2 <= nsm) cs <<= 1;
-    for (;; cs >>= 1) {
-      if (cs == 1) break;
-      cudaLaunchConfig_t cfg = {};
-      cudaLaunchAttribute attr[1];
-      attr[0].id = cudaLaunchAttributeClusterDimension;
-      attr[0].val.clusterDim.x = cs;
-      attr[0].val.clusterDim.y = 1;
-      attr[0].val.clusterDim.z = 1;
-      cfg.attrs = attr;
-      cfg.numAttrs = 1;
-      cfg.blockDim = dim3(nw * 32);
-      cfg.dynamicSmemBytes = (size_t)Lc.smem;
-      cfg.gridDim = dim3(P.ncell * cs);
-      int nclusters = 0;
-      if (cudaOccupancyMaxActiveClusters(&nclusters, elim_kernel, &cfg) == cudaSuccess && nclusters > 0) break;
-      cudaGetLastError();
+  struct Cell {
+    int start, count, lbound, cls;
+  };
+  auto size_class = [](int size) {
+    return size >= 1024 ? 4 : size >= 512 ? 3 : size >= 256 ? 2 : size >= 128 ? 1 : 0;
+  };
+  std::vector<std::vector<Cell>> step_cells;
+  std::vector<int> step_level;
+  int steps = 0;
+  for (int i = 0; i < K; i++) steps = std::max(steps, gs[i]->H - gs[i]->C);
+  for (int st = 0; st < steps; st++) {
+    std::vector<Cell> cells;
+    int level = 0;
+    for (int i = 0; i < K; i++) {
+      const Graph &g = *gs[i];
+      const int h = g.H - st;
+      if (h <= g.C) continue;
+      level = h;
+      const int64_t lo = (int64_t(1) << (h - 1)) - 1, hi = (int64_t(1) << h) - 2;
+      for (int64_t c = lo; c <= hi; c++) {
+        const int cnt = g.cell_count[c], lb = bound[i][c];
+        cells.push_back({vbase[i] + g.cell_start[c], cnt, lb, size_class(std::max(cnt, lb))});
+      }
     }
-    Lc.cs = cs;
-    if (Lc.global_stage)
-      pstage_ints = std::max<int64_t>(pstage_ints, (int64_t)P.ncell * cs * nw * 2 * (int64_t)P.lmax);
-    launches.push_back(Lc);
+    if (cells.empty()) continue;
+    step_cells.push_back(std::move(cells));
+    step_level.push_back(K > 1 ? -(st + 1) : level);  // a step, not one graph's level
+  }
+  {
+    std::vector<Cell> cells;
+    for (int i = 0; i < K; i++)
+      cells.push_back({vbase[i] + L[i].heap_start, L[i].heap_n, std::max(1, L[i].heap_n - 1),
+                       size_class(L[i].heap_n)});
+    step_cells.push_back(std::move(cells));
+    step_level.push_back(0);
+  }
+  const int nsteps = (int)step_cells.size();
+  std::vector<int> fcs, fcc;
+  auto al = [](int64_t bb) { return (bb + 15) & ~int64_t(15); };
+  int64_t pstage_ints = 0;
+  for (int st = 0; st < nsteps; st++) {
+    const bool heap = st == nsteps - 1;
+    std::vector<Cell> &cells = step_cells[st];
+    std::stable_sort(cells.begin(), cells.end(), [](const Cell &x, const Cell &y) { return x.cls > y.cls; });
+    int64_t step_pstage = 0;
+    for (size_t g0 = 0; g0 < cells.size();) {
+      size_t g1 = g0;
+      while (g1 < cells.size() && cells[g1].cls == cells[g0].cls) g1++;
+      Launch Lc;
+      Lc.step = st;
+      Lc.level = step_level[st];
+      Lc.heap = heap;
+      Lc.lo = (int64_t)fcs.size();
+      Lc.ncell = (int)(g1 - g0);
+      Lc.kmax = 1;
+      Lc.lmax = 1;
+      for (size_t c = g0; c < g1; c++) {
+        fcs.push_back(cells[c].start);
+        fcc.push_back(cells[c].count);
+        Lc.kmax = std::max(Lc.kmax, cells[c].count);
+        Lc.lmax = std::max(Lc.lmax, cells[c].lbound);
+      }
+      const int64_t keys_b = 3 * al(4LL * Lc.kmax);
+      const int64_t own_b = keys_b + 2 * al(4LL * Lc.lmax);
+      auto smem_for = [&](int w) { return own_b + 2 * al(4LL * Lc.lmax * w); };
+      int nw = Lc.ncell * 4 < nsm ? 16 : 8;
+      while (nw > 4 && smem_for(nw) > smem_dyn) nw >>= 1;
+      // per-warp merge buffers move to global memory when they do not fit
+      Lc.global_stage = smem_for(nw) > smem_dyn || force_global_stage;
+      if (Lc.global_stage) nw = Lc.ncell * 4 < nsm ? 16 : 8;
+      GH_CHECK(own_b <= smem_dyn, H2H_ERR_DEVICE,
+               "elimination staging does not fit shared memory (candidate keys + eliminated list too large)");
+      Lc.smem = Lc.global_stage ? own_b : smem_for(nw);
+      Lc.nw = nw;
+      // cluster size.  A cell eliminates serially; cs CTAs merge its lists
+      // about cs^a times faster, while cs times more CTAs compete for the
+      // resident slots.  Pick the cs that minimises waves(cs) / cs^a with
+      // waves = ceil(cells * cs / slots).  Measured on road graphs: a = 0.8
+      // above the bottom level; the bottom cells' vertices have few
+      // neighbours when eliminated, so extra CTAs mostly add barriers (a = 0.3).
+      const double alpha = st == 0 ? 0.3 : 0.8;
+      int per_sm = 0;
+      GH_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, elim_kernel, nw * 32, (size_t)Lc.smem));
+      const int64_t slots = (int64_t)std::max(1, per_sm) * nsm;
+      int cs = 1;
+      double best_cost = 1e300;
+      for (int c = 1; c <= 16; c <<= 1) {
+        const double waves = (double)((Lc.ncell * (int64_t)c + slots - 1) / slots);
+        const double cost = waves / std::pow((double)c, alpha);
+        if (cost < best_cost * 0.999) { best_cost = cost; cs = c; }
+      }
+      for (;; cs >>= 1) {
+        if (cs == 1) break;
+        cudaLaunchConfig_t cfg = {};
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = cs;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        cfg.blockDim = dim3(nw * 32);
+        cfg.dynamicSmemBytes = (size_t)Lc.smem;
+        cfg.gridDim = dim3(Lc.ncell * cs);
+        int nclusters = 0;
+        if (cudaOccupancyMaxActiveClusters(&nclusters, elim_kernel, &cfg) == cudaSuccess && nclusters > 0) break;
+        cudaGetLastError();
+      }
+      Lc.cs = cs;
+      Lc.pstage_off = step_pstage;
+      if (Lc.global_stage) step_pstage += (int64_t)Lc.ncell * cs * nw * 2 * (int64_t)Lc.lmax;
+      launches.push_back(Lc);
+      g0 = g1;
+    }
+    pstage_ints = std::max(pstage_ints, step_pstage);
+  }
+  {
+    // side streams for the groups of a step beyond the first
+    int most = 1;
+    for (int st = 0; st < nsteps; st++) {
+      int c = 0;
+      for (const Launch &Lc : launches) c += Lc.step == st;
+      most = std::max(most, c);
+    }
+    max_group = most;
   }
   // ---- device state
   try {
@@ -715,6 +800,15 @@ ElimPlan::ElimPlan(const std::vector<Graph *> &graphs) : gs(graphs) {
     adj_w = palloc<int>(std::max<int64_t>(M, 1), bytes);
     heap_verts = palloc<int>(std::max(heap_total, 1), bytes);
     if (pstage_ints) pstage = palloc<int>(pstage_ints, bytes);
+    for (int k = 1; k < max_group; k++) {
+      cudaStream_t st = nullptr;
+      cudaEvent_t e = nullptr;
+      GH_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+      side.push_back(st);
+      GH_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+      ev_join.push_back(e);
+    }
+    GH_CUDA(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
     GH_CUDA(cudaMemcpy(slot_off_init, f_slot_off.data(), sizeof(int64_t) * N, cudaMemcpyHostToDevice));
     GH_CUDA(cudaMemcpy(deg_init, f_deg.data(), sizeof(int) * N, cudaMemcpyHostToDevice));
     GH_CUDA(cudaMemcpy(cap_init, f_cap.data(), sizeof(int) * N, cudaMemcpyHostToDevice));
@@ -741,6 +835,12 @@ void ElimPlan::release() {
                 elim_init, deg0, deg_init, h0, cpos, err, ljunk, cell_start, cell_count, adj_off, adj_v, adj_w,
                 heap_verts, pstage};
   for (void *p : ps) cudaFree(p);
+  for (cudaStream_t st : side) cudaStreamDestroy(st);
+  for (cudaEvent_t e : ev_join) cudaEventDestroy(e);
+  if (ev_fork) cudaEventDestroy(ev_fork);
+  side.clear();
+  ev_join.clear();
+  ev_fork = nullptr;
   slot_nbr = slot_w = lsize = cap = cap_init = height = elim = elim_init = deg0 = deg_init = h0 = cpos = err = ljunk = nullptr;
   cell_start = cell_count = adj_off = adj_v = adj_w = heap_verts = pstage = nullptr;
   slot_off = slot_off_init = nullptr;
@@ -752,6 +852,42 @@ void ElimPlan::set_weights(int gi, const int *w, cudaStream_t s) {
   const Graph &g = *gs[gi];
   if (g.m)
     GH_CUDA(cudaMemcpyAsync(adj_w + mbase[gi], w, sizeof(int) * g.m, cudaMemcpyHostToDevice, s));
+}
+
+void ElimPlan::launch_one(const Launch &Lc, cudaStream_t s, bool trace) {
+  ElimArgs A;
+  A.slot_nbr = slot_nbr; A.slot_w = slot_w; A.slot_off = slot_off; A.lsize = lsize; A.ljunk = ljunk;
+  A.cap = cap; A.height = height; A.elim = elim; A.key_deg0 = deg0; A.key_h0 = Lc.heap ? h0 : nullptr;
+  A.cell_start = cell_start; A.cell_count = cell_count; A.cpos = cpos; A.err = err;
+  A.cell_lo = (int)Lc.lo; A.kmax = Lc.kmax; A.lmax = Lc.lmax; A.heap_mode = Lc.heap ? 1 : 0;
+  A.pool_next = pool_next; A.pool_size = pool_size;
+  A.pstage = Lc.global_stage ? pstage + Lc.pstage_off : nullptr;
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = Lc.cs;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  cfg.blockDim = dim3(Lc.nw * 32);
+  cfg.dynamicSmemBytes = (size_t)Lc.smem;
+  cfg.gridDim = dim3(Lc.ncell * Lc.cs);
+  cfg.stream = s;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  if (trace) { cudaEventCreate(&ev0); cudaEventCreate(&ev1); cudaEventRecord(ev0, s); }
+  GH_CUDA(cudaLaunchKernelEx(&cfg, elim_kernel, A));
+  if (trace) {
+    cudaEventRecord(ev1, s);
+    cudaEventSynchronize(ev1);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, ev0, ev1);
+    std::fprintf(stderr, "[gpuh2h] elim %s %d: %d cells x %d CTAs x %d warps, kmax %d, lmax %d, smem %lld%s: %.3f ms\n",
+                 Lc.heap ? "heap" : "level", Lc.level, Lc.ncell, Lc.cs, Lc.nw, Lc.kmax, Lc.lmax,
+                 (long long)Lc.smem, Lc.global_stage ? " (global merge staging)" : "", ms);
+    cudaEventDestroy(ev0);
+    cudaEventDestroy(ev1);
+  }
 }
 
 void ElimPlan::enqueue(cudaStream_t s, cudaEvent_t *heap_ev, bool trace) {
@@ -770,8 +906,11 @@ void ElimPlan::enqueue(cudaStream_t s, cudaEvent_t *heap_ev, bool trace) {
   scatter_adjacency_kernel<<<std::max(1, std::min(4096, (N + 255) / 256)), 256, 0, s>>>(
       adj_off, adj_v, adj_w, slot_off, slot_nbr, slot_w, N);
   GH_CUDA(cudaGetLastError());
-  for (const Launch &Lc : launches) {
-    if (Lc.heap) {
+  size_t li = 0;
+  while (li < launches.size()) {
+    size_t lj = li;
+    while (lj < launches.size() && launches[lj].step == launches[li].step) lj++;
+    if (launches[li].heap) {
       if (heap_ev) GH_CUDA(cudaEventRecord(heap_ev[0], s));
       if (heap_total) {
         prepare_heap_lists_kernel<<<std::max(1, std::min(4096, (heap_total * 32 + 255) / 256)), 256, 0, s>>>(
@@ -779,39 +918,19 @@ void ElimPlan::enqueue(cudaStream_t s, cudaEvent_t *heap_ev, bool trace) {
         GH_CUDA(cudaGetLastError());
       }
     }
-    ElimArgs A;
-    A.slot_nbr = slot_nbr; A.slot_w = slot_w; A.slot_off = slot_off; A.lsize = lsize; A.ljunk = ljunk;
-    A.cap = cap; A.height = height; A.elim = elim; A.key_deg0 = deg0; A.key_h0 = Lc.heap ? h0 : nullptr;
-    A.cell_start = cell_start; A.cell_count = cell_count; A.cpos = cpos; A.err = err;
-    A.cell_lo = (int)Lc.lo; A.kmax = Lc.kmax; A.lmax = Lc.lmax; A.heap_mode = Lc.heap ? 1 : 0;
-    A.pool_next = pool_next; A.pool_size = pool_size;
-    A.pstage = Lc.global_stage ? pstage : nullptr;
-    cudaLaunchConfig_t cfg = {};
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeClusterDimension;
-    attr[0].val.clusterDim.x = Lc.cs;
-    attr[0].val.clusterDim.y = 1;
-    attr[0].val.clusterDim.z = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    cfg.blockDim = dim3(Lc.nw * 32);
-    cfg.dynamicSmemBytes = (size_t)Lc.smem;
-    cfg.gridDim = dim3(Lc.ncell * Lc.cs);
-    cfg.stream = s;
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-    if (trace) { cudaEventCreate(&ev0); cudaEventCreate(&ev1); cudaEventRecord(ev0, s); }
-    GH_CUDA(cudaLaunchKernelEx(&cfg, elim_kernel, A));
-    if (trace) {
-      cudaEventRecord(ev1, s);
-      cudaEventSynchronize(ev1);
-      float ms = 0;
-      cudaEventElapsedTime(&ms, ev0, ev1);
-      std::fprintf(stderr, "[gpuh2h] elim %s %d: %d cells x %d CTAs x %d warps, kmax %d, lmax %d, smem %lld%s: %.3f ms\n",
-                   Lc.heap ? "heap" : "level", Lc.level, Lc.ncell, Lc.cs, Lc.nw, Lc.kmax, Lc.lmax,
-                   (long long)Lc.smem, Lc.global_stage ? " (global merge staging)" : "", ms);
-      cudaEventDestroy(ev0);
-      cudaEventDestroy(ev1);
+    // the groups of one step are independent: fork them onto side streams
+    if (lj - li > 1) GH_CUDA(cudaEventRecord(ev_fork, s));
+    for (size_t k = li; k < lj; k++) {
+      cudaStream_t ls = s;
+      if (k > li) {
+        ls = side[k - li - 1];
+        GH_CUDA(cudaStreamWaitEvent(ls, ev_fork, 0));
+      }
+      launch_one(launches[k], ls, trace);
+      if (k > li) GH_CUDA(cudaEventRecord(ev_join[k - li - 1], ls));
     }
+    for (size_t k = li + 1; k < lj; k++) GH_CUDA(cudaStreamWaitEvent(s, ev_join[k - li - 1], 0));
+    li = lj;
   }
   if (heap_ev) GH_CUDA(cudaEventRecord(heap_ev[1], s));
 }

@@ -33,10 +33,12 @@ struct DeviceIndex {
   int *dis = nullptr;         // padded labels          [dis_padded]
   int *father = nullptr;      // father                 [n]
   int *err = nullptr;         // kernel error word      [1]
-  int64_t bytes = 0;
-  std::vector<void *> owned;
+  int64_t bytes = 0, rmq_bytes = 0;
+  std::vector<void *> owned;      // label-side allocations of this handle
+  std::vector<void *> owned_rmq;  // first, rmq_hash, rmq_id (built with the tree)
   std::shared_ptr<void> keep;
   void release();
+  void release_labels();  // everything but the sparse table
 };
 
 struct Timings {
@@ -74,9 +76,8 @@ struct Graph {
   // tree (TreeStructure.cu)
   int head = -1, tree_height = 0;
   std::vector<int> father, depth, first, child_off, childs;
-  std::vector<int64_t> rmq_hash;
-  std::vector<int> rmq_id;
-  int64_t euler_n = 0, h2h_size = 0;
+  std::vector<int> euler_id;                // Euler tour (vertex per position), until the table is built
+  int64_t euler_n = 0, h2h_size = 0, rmq_total = 0;  // rmq_total: RMQ_ID entries (the table is on the GPU)
   // labels (H2HConsturction.cu), reference layout on the host
   std::vector<int64_t> dis_hash, pos_hash;
   std::vector<int> pos_id, pos_pos, pos_w;  // pos_w: shortcut weight per pos entry (0 for v itself)
@@ -101,8 +102,8 @@ struct Graph {
 // replayed (or captured in a CUDA graph) after set_weights().
 struct ElimPlan {
   struct Launch {
-    int level, ncell, kmax, lmax, cs, nw;
-    int64_t lo, smem;
+    int step, level, ncell, kmax, lmax, cs, nw;
+    int64_t lo, smem, pstage_off;
     bool heap, global_stage;
   };
   std::vector<Graph *> gs;
@@ -110,8 +111,11 @@ struct ElimPlan {
   std::vector<int64_t> mbase;
   int N = 0, heap_total = 0;
   int64_t M = 0, lub = 0, pool_size = 0;
-  std::vector<Launch> launches;
-  int nsm = 0;
+  std::vector<Launch> launches;  // in step order; launches of one step are independent
+  int nsm = 0, max_group = 1;
+  std::vector<cudaStream_t> side;  // streams for the second and later launches of a step
+  std::vector<cudaEvent_t> ev_join;
+  cudaEvent_t ev_fork = nullptr;
   // device state (global vertex ids)
   int *slot_nbr = nullptr, *slot_w = nullptr, *lsize = nullptr, *cap = nullptr, *cap_init = nullptr;
   int *height = nullptr, *elim = nullptr;
@@ -130,6 +134,7 @@ struct ElimPlan {
   // heap_ev non-null, records heap_ev[0] before the global-order launch and
   // heap_ev[1] after it.
   void enqueue(cudaStream_t s, cudaEvent_t *heap_ev = nullptr, bool trace = false);
+  void launch_one(const Launch &Lc, cudaStream_t s, bool trace);
   void check_error();  // synchronises; throws on a kernel error code
   // Elimination order, X(v) lists and their weights back into each graph.
   void download(bool weights_only = false);
@@ -191,7 +196,15 @@ void build_elimination_sets(Graph &g);                 // elim_sets.cpp
 // contract.cu: partition levels H..C+1 and the global heap over levels <= C;
 // fills g.elim (elimination order) and g.x_off / x_id / x_w
 void contract_gpu(Graph &g);
-void build_tree_and_rmq(Graph &g);                     // tree.cpp
+void build_tree(Graph &g);                             // tree.cpp: father, children, Euler tour
+// query.cu: the compacted sparse tables of the graphs' Euler tours on the
+// GPU (first, rmq_hash, rmq_id in each graph's DeviceIndex)
+void build_rmq_gpu(const std::vector<Graph *> &gs);
+void download_rmq(const Graph &g, int64_t *rmq_hash, int *rmq_id);  // query.cu
+inline void build_tree_and_rmq(Graph &g) {
+  build_tree(g);
+  build_rmq_gpu({&g});
+}
 void allocate_labels_and_bfs(Graph &g);                // tree.cpp
 void fill_labels_gpu(Graph &g);                        // labels.cu
 void download_labels(const Graph &g, int *dis_out);    // labels.cu, reference layout

@@ -25,16 +25,26 @@
 #include <sstream>
 
 #include "graph.h"
+#include "pool.h"
 
 namespace gh {
 
-void DeviceIndex::release() {
+void DeviceIndex::release_labels() {
   for (void *p : owned) cudaFree(p);
   owned.clear();
   keep.reset();
-  first = depth = rmq_id = pos_pos = pos_id = dis = father = err = nullptr;
-  rmq_hash = pos_hash = drow = nullptr;
-  bytes = 0;
+  depth = pos_pos = pos_id = dis = father = err = nullptr;
+  pos_hash = drow = nullptr;
+  bytes = rmq_bytes;
+}
+
+void DeviceIndex::release() {
+  release_labels();
+  for (void *p : owned_rmq) cudaFree(p);
+  owned_rmq.clear();
+  first = rmq_id = nullptr;
+  rmq_hash = nullptr;
+  bytes = rmq_bytes = 0;
 }
 
 namespace {
@@ -383,36 +393,53 @@ FillPlan::FillPlan(const std::vector<Graph *> &graphs, const TilePolicy &pol) : 
   const int K = (int)gs.size();
   GH_CHECK(K >= 1, H2H_ERR_ARG, "no graph to label");
   vbase.assign(K, 0);
+  std::vector<int64_t> pbase(K, 0), dbase(K, 0);
   for (int i = 0; i < K; i++) {
-    GH_CHECK((int64_t)N + gs[i]->n < INT32_MAX, H2H_ERR_ARG, "too many vertices in one batch");
+    const Graph &g = *gs[i];
+    GH_CHECK((int64_t)N + g.n < INT32_MAX, H2H_ERR_ARG, "too many vertices in one batch");
     vbase[i] = N;
-    N += gs[i]->n;
-    pos_total += gs[i]->pos_hash[gs[i]->n];
+    pbase[i] = pos_total;
+    dbase[i] = dis_total;
+    N += g.n;
+    pos_total += g.pos_hash[g.n];
+    for (int v = 0; v < g.n; v++) dis_total += (g.depth[v] + 3) & ~3;
   }
+  int host_threads = 1;
+  for (const Graph *g : gs) host_threads = std::max(host_threads, g->threads);
+  host_threads = std::min(host_threads, K);
   std::vector<int64_t> f_drow(N + 1, 0), f_pos_hash(N + 1, 0);
   std::vector<int> f_pos_pos(pos_total), f_pos_id(pos_total), f_pos_w(pos_total), f_pos_src(pos_total);
   std::vector<int> f_father(N), f_depth(N), f_nchild(N);
-  for (int i = 0; i < K; i++) {
-    const Graph &g = *gs[i];
-    const int vb = vbase[i];
-    const int64_t pb = f_pos_hash[vb];
-    for (int v = 0; v < g.n; v++) {
-      const int V = vb + v;
-      f_drow[V + 1] = f_drow[V] + ((g.depth[v] + 3) & ~3);
-      f_pos_hash[V + 1] = pb + g.pos_hash[v + 1];
-      f_father[V] = g.father[v] < 0 ? -1 : g.father[v] + vb;
-      f_depth[V] = g.depth[v];
-      f_nchild[V] = g.child_off[v + 1] - g.child_off[v];
-    }
-    const int64_t np = g.pos_hash[g.n];
-    for (int64_t k = 0; k < np; k++) {
-      f_pos_pos[pb + k] = g.pos_pos[k];
-      f_pos_id[pb + k] = g.pos_id[k] + vb;
-      f_pos_w[pb + k] = g.pos_w[k];
-      f_pos_src[pb + k] = g.pos_src.empty() ? -1 : g.pos_src[k];
-    }
+  {
+    Pool pool(host_threads);
+    pool.parallel_for(K, 1, [&](int64_t lo, int64_t hi, int) {
+      for (int64_t i = lo; i < hi; i++) {
+        const Graph &g = *gs[i];
+        const int vb = vbase[i];
+        const int64_t pb = pbase[i];
+        int64_t d = dbase[i];
+        for (int v = 0; v < g.n; v++) {
+          const int V = vb + v;
+          f_drow[V] = d;
+          d += (g.depth[v] + 3) & ~3;
+          f_pos_hash[V] = pb + g.pos_hash[v];
+          f_father[V] = g.father[v] < 0 ? -1 : g.father[v] + vb;
+          f_depth[V] = g.depth[v];
+          f_nchild[V] = g.child_off[v + 1] - g.child_off[v];
+        }
+        const int64_t np = g.pos_hash[g.n];
+        for (int64_t k = 0; k < np; k++) {
+          f_pos_pos[pb + k] = g.pos_pos[k];
+          f_pos_id[pb + k] = g.pos_id[k] + vb;
+          f_pos_w[pb + k] = g.pos_w[k];
+          f_pos_src[pb + k] = g.pos_src.empty() ? -1 : g.pos_src[k];
+        }
+      }
+    });
   }
-  dis_total = f_drow[N];
+  f_drow[N] = dis_total;
+  f_pos_hash[N] = pos_total;
+  threads = 128;
   int dev = 0;
   GH_CUDA(cudaGetDevice(&dev));
   GH_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
@@ -459,48 +486,100 @@ void FillPlan::release_work() {
 
 // Tiles in forest BFS order (level l of every graph, then level l + 1): a
 // node's father always holds an earlier ticket, so the dataflow cannot wait
-// on work no CTA has taken.
+// on work no CTA has taken.  Two passes over the graphs in parallel: tile
+// counts per (level, graph), then each graph writes its tiles at the
+// offsets the counts give.
 void FillPlan::build_tiles(const TilePolicy &pol) {
   policy = pol;
+  const int K = (int)gs.size();
   int nlev = 0;
   for (const Graph *g : gs) nlev = std::max(nlev, (int)g->tree_hash.size() - 1);
-  std::vector<int> tn, tc0, tc1, tu0, tu1, nt(N, 0);
-  max_u = 1;
-  max_c = 1;
-  for (int l = 0; l < nlev; l++) {
-    int64_t width = 0;
-    for (const Graph *g : gs)
-      if (l + 1 < (int)g->tree_hash.size()) width += g->tree_hash[l + 1] - g->tree_hash[l];
-    const int wb = width >= nsm ? 1 : 0;
-    for (size_t i = 0; i < gs.size(); i++) {
+  std::vector<int64_t> width(nlev, 0);
+  for (const Graph *g : gs)
+    for (int l = 0; l + 1 < (int)g->tree_hash.size(); l++) width[l] += g->tree_hash[l + 1] - g->tree_hash[l];
+  auto tiles_of = [&](int wb, int m, int d, int &nt_node, int &cb, int &sc) {
+    const int sb = TilePolicy::sep_bucket(m);
+    if ((int64_t)m * d <= pol.small_work[wb][sb]) {
+      nt_node = 1;
+      cb = d;
+      sc = std::max(m, 1);
+      return true;  // one tile
+    }
+    cb = pol.col_block[wb][sb];
+    sc = pol.sep_chunk[wb][sb];
+    nt_node = ((d + cb - 1) / cb) * ((std::max(m, 1) + sc - 1) / sc);
+    return false;
+  };
+  int host_threads = 1;
+  for (const Graph *g : gs) host_threads = std::max(host_threads, g->threads);
+  Pool pool(std::min(host_threads, K));
+  // pass 1: tiles per (level, graph), staging bounds per graph
+  std::vector<std::vector<int64_t>> cnt(K);
+  std::vector<int> mu(K, 1), mc(K, 1);
+  pool.parallel_for(K, 1, [&](int64_t lo, int64_t hi, int) {
+    for (int64_t i = lo; i < hi; i++) {
       const Graph &g = *gs[i];
-      if (l + 1 >= (int)g.tree_hash.size()) continue;
-      for (int q = g.tree_hash[l]; q < g.tree_hash[l + 1]; q++) {
-        const int v = g.tree_bfs[q], V = vbase[i] + v, d = g.depth[v];
-        const int m = (int)(g.pos_hash[v + 1] - g.pos_hash[v]) - 1;
-        const int sb = TilePolicy::sep_bucket(m);
-        if ((int64_t)m * d <= pol.small_work[wb][sb]) {
-          tn.push_back(V); tc0.push_back(0); tc1.push_back(d); tu0.push_back(0); tu1.push_back(m);
-          nt[V] = 1;
-          max_u = std::max(max_u, m);
-          max_c = std::max(max_c, d);
-        } else {
-          const int cb = pol.col_block[wb][sb], sc = pol.sep_chunk[wb][sb];
-          for (int c = 0; c < d; c += cb)
-            for (int u = 0; u < std::max(m, 1); u += sc) {
-              tn.push_back(V); tc0.push_back(c); tc1.push_back(std::min(d, c + cb));
-              tu0.push_back(u); tu1.push_back(std::min(m, u + sc));
-              nt[V]++;
-            }
-          max_u = std::max(max_u, std::min(m, sc));
-          max_c = std::max(max_c, std::min(d, cb));
+      const int gl = (int)g.tree_hash.size() - 1;
+      cnt[i].assign(gl, 0);
+      for (int l = 0; l < gl; l++) {
+        const int wb = width[l] >= nsm ? 1 : 0;
+        for (int q = g.tree_hash[l]; q < g.tree_hash[l + 1]; q++) {
+          const int v = g.tree_bfs[q], d = g.depth[v];
+          const int m = (int)(g.pos_hash[v + 1] - g.pos_hash[v]) - 1;
+          int nt_node, cb, sc;
+          const bool one = tiles_of(wb, m, d, nt_node, cb, sc);
+          cnt[i][l] += nt_node;
+          mu[i] = std::max(mu[i], one ? m : std::min(m, sc));
+          mc[i] = std::max(mc[i], one ? d : std::min(d, cb));
         }
       }
     }
-  }
-  ntiles = (int64_t)tn.size();
+  });
+  std::vector<std::vector<int64_t>> off(K);
+  int64_t total = 0;
+  for (int i = 0; i < K; i++) off[i].assign(cnt[i].size(), 0);
+  for (int l = 0; l < nlev; l++)
+    for (int i = 0; i < K; i++)
+      if (l < (int)cnt[i].size()) {
+        off[i][l] = total;
+        total += cnt[i][l];
+      }
+  ntiles = total;
   GH_CHECK(ntiles < INT32_MAX, H2H_ERR_ARG, "too many fill tiles");
-  const int64_t need = 5 * ntiles + N;  // node, c0, c1, u0, u1, then tiles per node
+  max_u = *std::max_element(mu.begin(), mu.end());
+  max_c = *std::max_element(mc.begin(), mc.end());
+  // pass 2: node, c0, c1, u0, u1 per tile, then tiles per node
+  std::vector<int> host((size_t)(5 * ntiles + N));
+  int *tn = host.data(), *tc0 = tn + ntiles, *tc1 = tn + 2 * ntiles, *tu0 = tn + 3 * ntiles,
+      *tu1 = tn + 4 * ntiles, *nt = tn + 5 * ntiles;
+  pool.parallel_for(K, 1, [&](int64_t lo, int64_t hi, int) {
+    for (int64_t i = lo; i < hi; i++) {
+      const Graph &g = *gs[i];
+      const int vb = vbase[i];
+      const int gl = (int)g.tree_hash.size() - 1;
+      for (int l = 0; l < gl; l++) {
+        const int wb = width[l] >= nsm ? 1 : 0;
+        int64_t t = off[i][l];
+        for (int q = g.tree_hash[l]; q < g.tree_hash[l + 1]; q++) {
+          const int v = g.tree_bfs[q], V = vb + v, d = g.depth[v];
+          const int m = (int)(g.pos_hash[v + 1] - g.pos_hash[v]) - 1;
+          int nt_node, cb, sc;
+          if (tiles_of(wb, m, d, nt_node, cb, sc)) {
+            tn[t] = V; tc0[t] = 0; tc1[t] = d; tu0[t] = 0; tu1[t] = m;
+            t++;
+          } else {
+            for (int c = 0; c < d; c += cb)
+              for (int u = 0; u < std::max(m, 1); u += sc) {
+                tn[t] = V; tc0[t] = c; tc1[t] = std::min(d, c + cb); tu0[t] = u; tu1[t] = std::min(m, u + sc);
+                t++;
+              }
+          }
+          nt[V] = nt_node;
+        }
+      }
+    }
+  });
+  const int64_t need = 5 * ntiles + N;
   if (need > tiles_cap) {
     cudaFree(tiles);
     tiles = nullptr;
@@ -508,10 +587,7 @@ void FillPlan::build_tiles(const TilePolicy &pol) {
     tiles = dalloc<int>(need, work_bytes);
     tiles_cap = need;
   }
-  const std::vector<int> *parts[5] = {&tn, &tc0, &tc1, &tu0, &tu1};
-  for (int k = 0; k < 5; k++)
-    GH_CUDA(cudaMemcpy(tiles + k * ntiles, parts[k]->data(), sizeof(int) * ntiles, cudaMemcpyHostToDevice));
-  GH_CUDA(cudaMemcpy(tiles + 5 * ntiles, nt.data(), sizeof(int) * N, cudaMemcpyHostToDevice));
+  GH_CUDA(cudaMemcpy(tiles, host.data(), sizeof(int) * need, cudaMemcpyHostToDevice));
   const int smem_dyn = enable_max_dynamic_smem(fill_flow_kernel);
   smem = (size_t)max_u * 16 + (size_t)max_c * 8;
   GH_CHECK(smem <= (size_t)smem_dyn, H2H_ERR_DEVICE, "separator or tree too large for the fill staging");
@@ -584,7 +660,7 @@ void FillPlan::attach(bool first) {
     DeviceIndex &D = g.dev;
     const int vb = vbase[i];
     if (first) {
-      D.release();
+      D.release_labels();
       D.n = g.n;
       D.keep = storage;
       D.depth = depth + vb;
@@ -728,7 +804,7 @@ void fill_labels_gpu(Graph &g) {
     plan.attach(true);
     return;
   }
-  D.release();
+  D.release_labels();
   D.n = n;
   // padded row offsets
   std::vector<int64_t> drow(n + 1, 0);

@@ -159,20 +159,148 @@ __global__ void __launch_bounds__(256, 8) query_tile_kernel(QArgs A) {
 
 }  // namespace
 
+// ---- compacted sparse table of the Euler tour (makeOULAAndRMQ,
+// TreeStructure.cu:500-572), built on the GPU.  Row i of the table holds the
+// shallowest-node ids of the windows [i, i + 2^j) for every j with
+// i + 2^j - 1 < L, so it has floor(log2(L - i)) + 1 entries and starts at
+//   RMQHash[i] = S(L) - S(L - i),  S(x) = sum_{t=1..x} (floor(log2 t) + 1)
+//              = (k - 1) 2^k + 1 + (x - 2^k + 1)(k + 1),  k = floor(log2 x).
+// Level j combines two level-(j-1) windows, the left one winning ties
+// (depth <=, TreeStructure.cu:528); one launch per level covers the Euler
+// tours of every graph given.
+namespace {
+
+struct RmqJob {
+  const int *eid;    // Euler tour, vertex per position
+  const int *depth;  // depth per vertex
+  int64_t *hash;     // RMQHash [L]
+  int *id;           // RMQ_ID  [S(L)]
+  int64_t L;
+};
+
+__host__ __device__ inline int64_t rmq_prefix(int64_t x) {
+  if (x <= 0) return 0;
+  int k = 0;
+  while ((int64_t(2) << k) <= x) k++;
+  return ((int64_t)(k - 1) << k) + 1 + (x - (int64_t(1) << k) + 1) * (k + 1);
+}
+
+__device__ __forceinline__ int job_of(const int64_t *off, int njobs, int64_t p) {
+  int lo = 0, hi = njobs - 1;  // last job with off[job] <= p
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (off[mid] <= p) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+__global__ void rmq_hash_kernel(const RmqJob *jobs, const int64_t *off, int njobs, int64_t total) {
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < total; p += (int64_t)gridDim.x * blockDim.x) {
+    const int g = job_of(off, njobs, p);
+    const int64_t i = p - off[g], L = jobs[g].L;
+    jobs[g].hash[i] = rmq_prefix(L) - rmq_prefix(L - i);
+  }
+}
+
+__global__ void rmq_level_kernel(const RmqJob *jobs, const int64_t *off, int njobs, int64_t total, int j) {
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < total; p += (int64_t)gridDim.x * blockDim.x) {
+    const int g = job_of(off, njobs, p);
+    const RmqJob J = jobs[g];
+    const int64_t i = p - off[g];
+    if (j == 0) {
+      J.id[J.hash[i]] = J.eid[i];
+    } else if (i + (int64_t(1) << j) - 1 < J.L) {
+      const int a = J.id[J.hash[i] + j - 1];
+      const int c = J.id[J.hash[i + (int64_t(1) << (j - 1))] + j - 1];
+      J.id[J.hash[i] + j] = __ldg(J.depth + a) <= __ldg(J.depth + c) ? a : c;
+    }
+  }
+}
+
+}  // namespace
+
+void build_rmq_gpu(const std::vector<Graph *> &gs) {
+  Clock clk;
+  const int K = (int)gs.size();
+  std::vector<int64_t> off(K + 1, 0), voff(K + 1, 0);
+  int levels = 0;
+  for (int i = 0; i < K; i++) {
+    const Graph &g = *gs[i];
+    GH_CHECK((int64_t)g.euler_id.size() == g.euler_n && g.euler_n == 2 * (int64_t)g.n - 1, H2H_ERR_STATE,
+             "Euler tour missing");
+    off[i + 1] = off[i] + g.euler_n;
+    voff[i + 1] = voff[i] + g.n;
+    levels = std::max(levels, ilog2_floor(g.euler_n));
+  }
+  const int64_t total = off[K];
+  int64_t tmp = 0;
+  int *d_eid = nullptr, *d_depth = nullptr;
+  int64_t *d_off = nullptr;
+  RmqJob *d_jobs = nullptr;
+  auto cleanup = [&]() { cudaFree(d_eid); cudaFree(d_depth); cudaFree(d_off); cudaFree(d_jobs); };
+  try {
+    d_eid = dalloc<int>(total, tmp);
+    d_depth = dalloc<int>(voff[K], tmp);
+    d_off = dalloc<int64_t>(K + 1, tmp);
+    d_jobs = dalloc<RmqJob>(K, tmp);
+    std::vector<RmqJob> jobs(K);
+    for (int i = 0; i < K; i++) {
+      Graph &g = *gs[i];
+      DeviceIndex &D = g.dev;
+      for (void *p : D.owned_rmq) cudaFree(p);
+      D.owned_rmq.clear();
+      D.bytes -= D.rmq_bytes;
+      D.rmq_bytes = 0;
+      D.euler = g.euler_n;
+      g.rmq_total = rmq_prefix(g.euler_n);
+      D.rmq = g.rmq_total;
+      D.first = dalloc<int>(g.n, D.rmq_bytes);
+      D.owned_rmq.push_back(D.first);
+      D.rmq_hash = dalloc<int64_t>(D.euler, D.rmq_bytes);
+      D.owned_rmq.push_back(D.rmq_hash);
+      D.rmq_id = dalloc<int>(D.rmq, D.rmq_bytes);
+      D.owned_rmq.push_back(D.rmq_id);
+      D.bytes += D.rmq_bytes;
+      GH_CUDA(cudaMemcpy(D.first, g.first.data(), sizeof(int) * g.n, cudaMemcpyHostToDevice));
+      GH_CUDA(cudaMemcpy(d_eid + off[i], g.euler_id.data(), sizeof(int) * g.euler_n, cudaMemcpyHostToDevice));
+      GH_CUDA(cudaMemcpy(d_depth + voff[i], g.depth.data(), sizeof(int) * g.n, cudaMemcpyHostToDevice));
+      jobs[i] = RmqJob{d_eid + off[i], d_depth + voff[i], D.rmq_hash, D.rmq_id, g.euler_n};
+    }
+    GH_CUDA(cudaMemcpy(d_jobs, jobs.data(), sizeof(RmqJob) * K, cudaMemcpyHostToDevice));
+    GH_CUDA(cudaMemcpy(d_off, off.data(), sizeof(int64_t) * (K + 1), cudaMemcpyHostToDevice));
+    int dev = 0, nsm = 0;
+    GH_CUDA(cudaGetDevice(&dev));
+    GH_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)nsm * 8, (total + 255) / 256));
+    rmq_hash_kernel<<<blocks, 256>>>(d_jobs, d_off, K, total);
+    GH_CUDA(cudaGetLastError());
+    for (int j = 0; j <= levels; j++) {
+      rmq_level_kernel<<<blocks, 256>>>(d_jobs, d_off, K, total, j);
+      GH_CUDA(cudaGetLastError());
+    }
+    GH_CUDA(cudaDeviceSynchronize());
+  } catch (...) {
+    cleanup();
+    throw;
+  }
+  cleanup();
+  const long long us = clk.us();
+  for (Graph *g : gs) {
+    std::vector<int>().swap(g->euler_id);
+    g->t.tree += us / K;
+  }
+}
+
+void download_rmq(const Graph &g, int64_t *rmq_hash, int *rmq_id) {
+  GH_CHECK(g.dev.rmq_hash && g.dev.rmq_id, H2H_ERR_STATE, "sparse table not built");
+  if (rmq_hash) GH_CUDA(cudaMemcpy(rmq_hash, g.dev.rmq_hash, sizeof(int64_t) * g.euler_n, cudaMemcpyDeviceToHost));
+  if (rmq_id) GH_CUDA(cudaMemcpy(rmq_id, g.dev.rmq_id, sizeof(int) * g.rmq_total, cudaMemcpyDeviceToHost));
+}
+
+// The sparse table and firstAppeare are on the device since h2h_contract;
+// labels since the fill.  Nothing is left to upload.
 void upload_query_index(Graph &g) {
-  DeviceIndex &D = g.dev;
-  const int n = g.n;
-  D.euler = g.euler_n;
-  D.rmq = (int64_t)g.rmq_id.size();
-  D.first = dalloc<int>(n, D.bytes);
-  D.owned.push_back(D.first);
-  D.rmq_hash = dalloc<int64_t>(D.euler, D.bytes);
-  D.owned.push_back(D.rmq_hash);
-  D.rmq_id = dalloc<int>(D.rmq, D.bytes);
-  D.owned.push_back(D.rmq_id);
-  GH_CUDA(cudaMemcpy(D.first, g.first.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
-  GH_CUDA(cudaMemcpy(D.rmq_hash, g.rmq_hash.data(), sizeof(int64_t) * D.euler, cudaMemcpyHostToDevice));
-  GH_CUDA(cudaMemcpy(D.rmq_id, g.rmq_id.data(), sizeof(int) * D.rmq, cudaMemcpyHostToDevice));
+  GH_CHECK(g.dev.first && g.dev.rmq_hash && g.dev.rmq_id, H2H_ERR_STATE, "sparse table not built");
 }
 
 void run_query_batch(const Graph &g, const int *x, const int *y, int *out, int64_t n, int mode, cudaStream_t s) {

@@ -17,7 +17,7 @@
 
 namespace gh {
 
-void build_tree_and_rmq(Graph &g) {
+void build_tree(Graph &g) {
   Clock clk;
   const int n = g.n;
   std::vector<int> rank(n, -1);
@@ -42,7 +42,7 @@ void build_tree_and_rmq(Graph &g) {
   GH_CHECK(g.child_off[n] == n - 1, H2H_ERR_STATE, "decomposition is not a single tree");
   // Euler tour
   const int64_t L = 2 * (int64_t)n - 1;
-  std::vector<int> eid(L), edep(L);
+  std::vector<int> eid(L);
   g.first.assign(n, -1);
   g.depth.assign(n, -1);
   std::vector<int> stk, cur;
@@ -53,7 +53,7 @@ void build_tree_and_rmq(Graph &g) {
   g.tree_height = 0;
   stk.push_back(g.head);
   cur.push_back(0);
-  eid[e] = g.head; edep[e] = 1; g.first[g.head] = 0; e++;
+  eid[e] = g.head; g.first[g.head] = 0; e++;
   g.depth[g.head] = 1;
   g.h2h_size = 1;
   g.tree_height = 1;
@@ -64,7 +64,7 @@ void build_tree_and_rmq(Graph &g) {
       int ch = g.childs[g.child_off[v] + c];
       c++;
       int d = (int)stk.size() + 1;
-      eid[e] = ch; edep[e] = d; g.first[ch] = (int)e; e++;
+      eid[e] = ch; g.first[ch] = (int)e; e++;
       g.depth[ch] = d;
       g.h2h_size += d;
       g.tree_height = std::max(g.tree_height, d);
@@ -73,35 +73,12 @@ void build_tree_and_rmq(Graph &g) {
     } else {
       stk.pop_back();
       cur.pop_back();
-      if (!stk.empty()) { eid[e] = stk.back(); edep[e] = (int)stk.size(); e++; }
+      if (!stk.empty()) { eid[e] = stk.back(); e++; }
     }
   }
   GH_CHECK(e == L, H2H_ERR_STATE, "Euler tour does not cover the tree");
   g.euler_n = L;
-  // compacted sparse table
-  g.rmq_hash.resize(L);
-  int64_t tot = 0;
-  for (int64_t i = 0; i < L; i++) { g.rmq_hash[i] = tot; tot += ilog2_floor(L - i) + 1; }
-  g.rmq_id.resize(tot);
-  Pool pool(g.threads);
-  std::vector<int> prev(eid), nxt(L);
-  pool.parallel_for(L, 1 << 16, [&](int64_t b, int64_t en, int) {
-    for (int64_t i = b; i < en; i++) g.rmq_id[g.rmq_hash[i]] = eid[i];
-  });
-  const int levels = ilog2_floor(L);
-  for (int j = 1; j <= levels; j++) {
-    const int64_t half = int64_t(1) << (j - 1);
-    const int64_t cnt_j = L - (int64_t(1) << j) + 1;  // rows with i + 2^j - 1 < L
-    pool.parallel_for(cnt_j, 1 << 16, [&](int64_t b, int64_t en, int) {
-      for (int64_t i = b; i < en; i++) {
-        int a = prev[i], c = prev[i + half];
-        int r = g.depth[a] <= g.depth[c] ? a : c;
-        nxt[i] = r;
-        g.rmq_id[g.rmq_hash[i] + j] = r;
-      }
-    });
-    prev.swap(nxt);
-  }
+  g.euler_id.swap(eid);
   g.t.tree = clk.us();
 }
 
