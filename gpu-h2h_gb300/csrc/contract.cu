@@ -723,19 +723,21 @@ ElimPlan::ElimPlan(const std::vector<Graph *> &graphs) : gs(graphs) {
       Lc.nw = nw;
       // cluster size.  A cell eliminates serially; cs CTAs merge its lists
       // about cs^a times faster, while cs times more CTAs compete for the
-      // resident slots.  Pick the cs that minimises waves(cs) / cs^a with
-      // waves = ceil(cells * cs / slots).  Measured on road graphs: a = 0.8
+      // resident slots.  Pick the cs that minimises waves(cs)^1.2 / cs^a with
+      // waves = ceil(cells * cs / slots) (a later wave also waits for the
+      // slowest cell of the one before).  Measured on road graphs: a = 0.8
       // above the bottom level; the bottom cells' vertices have few
       // neighbours when eliminated, so extra CTAs mostly add barriers (a = 0.3).
       const double alpha = st == 0 ? 0.3 : 0.8;
       int per_sm = 0;
       GH_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, elim_kernel, nw * 32, (size_t)Lc.smem));
       const int64_t slots = (int64_t)std::max(1, per_sm) * nsm;
+      Lc.slots = (int)slots;
       int cs = 1;
       double best_cost = 1e300;
       for (int c = 1; c <= 16; c <<= 1) {
         const double waves = (double)((Lc.ncell * (int64_t)c + slots - 1) / slots);
-        const double cost = waves / std::pow((double)c, alpha);
+        const double cost = std::pow(waves, 1.2) / std::pow((double)c, alpha);
         if (cost < best_cost * 0.999) { best_cost = cost; cs = c; }
       }
       for (;; cs >>= 1) {
@@ -882,9 +884,10 @@ void ElimPlan::launch_one(const Launch &Lc, cudaStream_t s, bool trace) {
     cudaEventSynchronize(ev1);
     float ms = 0;
     cudaEventElapsedTime(&ms, ev0, ev1);
-    std::fprintf(stderr, "[gpuh2h] elim %s %d: %d cells x %d CTAs x %d warps, kmax %d, lmax %d, smem %lld%s: %.3f ms\n",
-                 Lc.heap ? "heap" : "level", Lc.level, Lc.ncell, Lc.cs, Lc.nw, Lc.kmax, Lc.lmax,
-                 (long long)Lc.smem, Lc.global_stage ? " (global merge staging)" : "", ms);
+    std::fprintf(stderr,
+                 "[gpuh2h] elim %s %d: %d cells x %d CTAs x %d warps, kmax %d, lmax %d, smem %lld, slots %d%s: %.3f ms\n",
+                 Lc.heap ? "heap" : "level", Lc.level, Lc.ncell, Lc.cs, Lc.nw, Lc.kmax, Lc.lmax, (long long)Lc.smem,
+                 Lc.slots, Lc.global_stage ? " (global merge staging)" : "", ms);
     cudaEventDestroy(ev0);
     cudaEventDestroy(ev1);
   }

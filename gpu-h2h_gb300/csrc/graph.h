@@ -84,6 +84,14 @@ struct Graph {
   std::vector<int> pos_src;                 // index of the pos entry in v's X list (-1 for v itself)
   std::vector<int64_t> drow_host;           // padded device row offsets (absolute in a batch's forest)
   std::vector<int> tree_bfs, tree_hash;     // TreeBFS / TreeHash
+  // heavy-path decomposition of the tree for ancestor lookups in the fill:
+  // hld lists the heavy paths one after another, top to bottom (hpos[v] =
+  // v's index, htop[v] = the top of v's path); node v's root path is the
+  // segments seg_off[v] .. seg_off[v+1]-1, shallowest first, one per heavy
+  // path it crosses (written on the GPU by FillPlan)
+  std::vector<int> hld, htop, hpos;
+  std::vector<int64_t> seg_off;
+  int max_segs = 0;
   bool labelled = false;
   int64_t max_label = 0;
   // device
@@ -102,7 +110,7 @@ struct Graph {
 // replayed (or captured in a CUDA graph) after set_weights().
 struct ElimPlan {
   struct Launch {
-    int step, level, ncell, kmax, lmax, cs, nw;
+    int step, level, ncell, kmax, lmax, cs, nw, slots;
     int64_t lo, smem, pstage_off;
     bool heap, global_stage;
   };
@@ -170,9 +178,11 @@ struct FillPlan {
   int *pos_pos = nullptr, *pos_id = nullptr, *pos_w = nullptr, *pos_src = nullptr, *father = nullptr;
   int *depth = nullptr, *dis = nullptr;
   // workspace
-  int *nchild = nullptr, *chain = nullptr, *done = nullptr, *next = nullptr, *err = nullptr, *tiles = nullptr;
+  int *hld = nullptr, *htop = nullptr, *hpos = nullptr, *seg_top = nullptr, *seg_pos = nullptr;
+  int64_t *seg_off = nullptr;
+  int *done = nullptr, *next = nullptr, *err = nullptr, *tiles = nullptr;
   int64_t ntiles = 0, tiles_cap = 0;
-  int max_u = 1, max_c = 1, blocks = 1, threads = 128;
+  int max_u = 1, max_c = 1, max_segs = 1, blocks = 1, threads = 128;
   size_t smem = 0;
   int nsm = 0;
   int64_t work_bytes = 0;

@@ -180,12 +180,15 @@ __global__ void fill_level_kernel(FillArgs A) {
 // for the father's flag alone: no level barriers, so the thin top of the
 // tree pipelines with the wide middle.  A CTA spins on the flag with an
 // acquire load, a nanosleep back-off and a clock limit (on expiry it records
-// an error and stops); rows and chains produced in this launch are read
-// through L2 (ld.global.cg) so no stale L1 line is used.
+// an error and stops); rows produced in this launch are read through L2
+// (ld.global.cg) so no stale L1 line is used.
 //
-// Each node also publishes its ancestor chain (ids of the ancestors at depth
-// 1..d-1, then itself) in a scratch array laid out like the labels, so its
-// children can locate the rows a_j without walking father pointers.
+// The ancestor a_j of a column comes from the tree's heavy-path layout: the
+// node's root path is a handful of heavy-path segments (at most one more
+// than the light edges above it, so O(log n)), staged in shared memory; a
+// short search finds the segment holding depth j+1 and the path array gives
+// the node.  No per-node ancestor list is stored.
+//
 // Bound on one dependency wait, in SM clock cycles: 2 s at 2 GHz, or
 // GPUH2H_SPIN_LIMIT_MS (profilers replay instrumented kernels much slower).
 long long spin_limit_cycles() {
@@ -203,20 +206,21 @@ struct FlowArgs {
   int *node_cnt;           // finished tiles per node
   const int *father;
   const int *depth;
-  const int *nchild;
   const int64_t *drow;
   int *dis;
   const int64_t *pos_hash;
   const int *pos_id;
   const int *pos_pos;
   const int *pos_w;
-  int *chain;         // per node row: ancestor ids then the node itself
-  int *done;          // per vertex: 1 once its row and chain are visible
+  const int *hld;          // heavy paths, top to bottom
+  const int64_t *seg_off;  // root-path segments per node
+  const int *seg_top, *seg_pos;
+  int *done;          // per vertex: 1 once its row is visible
   int *next;          // work counter
   int *err;           // 0 = ok, 4 = a wait ran out
   long long spin_limit;
   int max_u;          // max separator members in one tile (staging size)
-  int max_c;          // max columns in one tile (staging size)
+  int max_segs;       // max root-path segments of a node (staging size)
 };
 
 __device__ __forceinline__ int ld_acquire(const int *p) {
@@ -238,9 +242,10 @@ __global__ void __launch_bounds__(128) fill_flow_kernel(FlowArgs A) {
   __shared__ int s_t, s_stop;
   const int tid = threadIdx.x, T = blockDim.x;
   int64_t *xs_row = (int64_t *)smem;                 // [max_u]
-  int64_t *anc_row = xs_row + A.max_u;               // [max_c]
-  int *xs_p = (int *)(anc_row + A.max_c);            // [max_u]
+  int *xs_p = (int *)(xs_row + A.max_u);             // [max_u]
   int *xs_w = xs_p + A.max_u;                        // [max_u]
+  int *s_top = xs_w + A.max_u;                       // [max_segs]
+  int *s_pos = s_top + A.max_segs;                   // [max_segs]
   for (;;) {
     if (tid == 0) s_t = atomicAdd(A.next, 1);
     __syncthreads();
@@ -265,37 +270,38 @@ __global__ void __launch_bounds__(128) fill_flow_kernel(FlowArgs A) {
         }
       }
     }
-    __syncthreads();
-    if (s_stop) return;
     const int64_t base = __ldg(A.drow + v);
     const int64_t pb = __ldg(A.pos_hash + v);
     const int m = (int)(__ldg(A.pos_hash + v + 1) - pb) - 1;   // X(v)\{v}
     const bool whole_sep = u0 == 0 && u1 == m;                  // this tile sees every member
     const int nu = u1 - u0;
+    // separator entries and the root-path segments need no finished row:
+    // stage them while thread 0 waits
     for (int i = tid; i < nu; i += T) {
       xs_p[i] = __ldg(A.pos_pos + pb + u0 + i);
       xs_w[i] = __ldg(A.pos_w + pb + u0 + i);
       xs_row[i] = __ldg(A.drow + __ldg(A.pos_id + pb + u0 + i));
     }
-    // ancestor chain for this tile's columns, from the father's published chain
-    const bool publish = u0 == 0 && __ldg(A.nchild + v) > 0;
-    const int cend = min(c1, d - 1);
-    if (d >= 2) {
-      const int64_t fb = __ldg(A.drow + f);
-      for (int j = c0 + tid; j < cend; j += T) {
-        const int a = __ldcg(A.chain + fb + j);
-        anc_row[j - c0] = __ldg(A.drow + a);
-        if (publish) A.chain[base + j] = a;
-      }
+    const int64_t sb = __ldg(A.seg_off + v);
+    const int ns = (int)(__ldg(A.seg_off + v + 1) - sb);
+    for (int i = tid; i < ns; i += T) {
+      s_top[i] = __ldg(A.seg_top + sb + i);
+      s_pos[i] = __ldg(A.seg_pos + sb + i);
     }
-    if (tid == 0 && c1 == d && u0 == 0) {
-      A.dis[base + d - 1] = 0;
-      if (publish) A.chain[base + d - 1] = v;
-    }
+    if (tid == 0 && c1 == d && u0 == 0) A.dis[base + d - 1] = 0;
     __syncthreads();
+    if (s_stop) return;
+    const int cend = min(c1, d - 1);
     for (int j = c0 + tid; j < cend; j += T) {
+      // ancestor at depth j + 1: last segment whose top depth is <= j + 1
+      int lo = 0, hi = ns - 1;
+      while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (s_top[mid] <= j + 1) lo = mid; else hi = mid - 1;
+      }
+      const int a = __ldg(A.hld + s_pos[lo] + (j + 1 - s_top[lo]));
+      const int64_t arow = __ldg(A.drow + a);
       int r = INT_MAX;
-      const int64_t arow = anc_row[j - c0];
 #pragma unroll 8
       for (int i = 0; i < nu; i++) {
         const int p = xs_p[i];
@@ -316,6 +322,24 @@ __global__ void __launch_bounds__(128) fill_flow_kernel(FlowArgs A) {
         __threadfence();
         st_release(A.done + v, 1);
       }
+    }
+  }
+}
+
+// Root-path segments of every node, shallowest first: walking up from v,
+// each heavy path met contributes (depth of its top, index of its top in
+// hld).  One thread per node; the walk crosses O(log n) light edges.
+__global__ void root_path_segments_kernel(const int *father, const int *depth, const int *htop, const int *hpos,
+                                          const int64_t *seg_off, int *seg_top, int *seg_pos, int n) {
+  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
+    const int64_t b = seg_off[v];
+    int64_t k = seg_off[v + 1];
+    for (int u = v; u >= 0 && k > b;) {
+      const int t = htop[u];
+      --k;
+      seg_top[k] = depth[t];
+      seg_pos[k] = hpos[t];
+      u = father[t];
     }
   }
 }
@@ -409,7 +433,16 @@ FillPlan::FillPlan(const std::vector<Graph *> &graphs, const TilePolicy &pol) : 
   host_threads = std::min(host_threads, K);
   std::vector<int64_t> f_drow(N + 1, 0), f_pos_hash(N + 1, 0);
   std::vector<int> f_pos_pos(pos_total), f_pos_id(pos_total), f_pos_w(pos_total), f_pos_src(pos_total);
-  std::vector<int> f_father(N), f_depth(N), f_nchild(N);
+  std::vector<int> f_father(N), f_depth(N), f_hld(N);
+  std::vector<int64_t> sbase(K, 0);
+  int64_t seg_total = 0;
+  for (int i = 0; i < K; i++) {
+    sbase[i] = seg_total;
+    seg_total += gs[i]->seg_off[gs[i]->n];
+    max_segs = std::max(max_segs, gs[i]->max_segs);
+  }
+  std::vector<int64_t> f_seg_off(N + 1, 0);
+  std::vector<int> f_htop(N), f_hpos(N);
   {
     Pool pool(host_threads);
     pool.parallel_for(K, 1, [&](int64_t lo, int64_t hi, int) {
@@ -425,7 +458,10 @@ FillPlan::FillPlan(const std::vector<Graph *> &graphs, const TilePolicy &pol) : 
           f_pos_hash[V] = pb + g.pos_hash[v];
           f_father[V] = g.father[v] < 0 ? -1 : g.father[v] + vb;
           f_depth[V] = g.depth[v];
-          f_nchild[V] = g.child_off[v + 1] - g.child_off[v];
+          f_hld[V] = g.hld[v] + vb;
+          f_htop[V] = g.htop[v] + vb;
+          f_hpos[V] = g.hpos[v] + vb;
+          f_seg_off[V] = sbase[i] + g.seg_off[v];
         }
         const int64_t np = g.pos_hash[g.n];
         for (int64_t k = 0; k < np; k++) {
@@ -439,6 +475,7 @@ FillPlan::FillPlan(const std::vector<Graph *> &graphs, const TilePolicy &pol) : 
   }
   f_drow[N] = dis_total;
   f_pos_hash[N] = pos_total;
+  f_seg_off[N] = seg_total;
   threads = 128;
   int dev = 0;
   GH_CUDA(cudaGetDevice(&dev));
@@ -455,8 +492,12 @@ FillPlan::FillPlan(const std::vector<Graph *> &graphs, const TilePolicy &pol) : 
   try {
     pos_w = dalloc<int>(pos_total, work_bytes);
     pos_src = dalloc<int>(pos_total, work_bytes);
-    nchild = dalloc<int>(N, work_bytes);
-    chain = dalloc<int>(dis_total, work_bytes);
+    hld = dalloc<int>(N, work_bytes);
+    htop = dalloc<int>(N, work_bytes);
+    hpos = dalloc<int>(N, work_bytes);
+    seg_off = dalloc<int64_t>(N + 1, work_bytes);
+    seg_top = dalloc<int>(std::max<int64_t>(seg_total, 1), work_bytes);
+    seg_pos = dalloc<int>(std::max<int64_t>(seg_total, 1), work_bytes);
     done = dalloc<int>(2 * (int64_t)N, work_bytes);  // done flags, then per-node tile counters
     next = dalloc<int>(1, work_bytes);
     err = dalloc<int>(1, work_bytes);
@@ -468,7 +509,13 @@ FillPlan::FillPlan(const std::vector<Graph *> &graphs, const TilePolicy &pol) : 
     GH_CUDA(cudaMemcpy(pos_src, f_pos_src.data(), sizeof(int) * pos_total, cudaMemcpyHostToDevice));
     GH_CUDA(cudaMemcpy(father, f_father.data(), sizeof(int) * N, cudaMemcpyHostToDevice));
     GH_CUDA(cudaMemcpy(depth, f_depth.data(), sizeof(int) * N, cudaMemcpyHostToDevice));
-    GH_CUDA(cudaMemcpy(nchild, f_nchild.data(), sizeof(int) * N, cudaMemcpyHostToDevice));
+    GH_CUDA(cudaMemcpy(hld, f_hld.data(), sizeof(int) * N, cudaMemcpyHostToDevice));
+    GH_CUDA(cudaMemcpy(seg_off, f_seg_off.data(), sizeof(int64_t) * (N + 1), cudaMemcpyHostToDevice));
+    GH_CUDA(cudaMemcpy(htop, f_htop.data(), sizeof(int) * N, cudaMemcpyHostToDevice));
+    GH_CUDA(cudaMemcpy(hpos, f_hpos.data(), sizeof(int) * N, cudaMemcpyHostToDevice));
+    root_path_segments_kernel<<<std::max(1, std::min(8192, (N + 255) / 256)), 256>>>(father, depth, htop, hpos,
+                                                                                     seg_off, seg_top, seg_pos, N);
+    GH_CUDA(cudaGetLastError());
     build_tiles(pol);
   } catch (...) {
     release_work();
@@ -479,9 +526,10 @@ FillPlan::FillPlan(const std::vector<Graph *> &graphs, const TilePolicy &pol) : 
 FillPlan::~FillPlan() { release_work(); }
 
 void FillPlan::release_work() {
-  void *ps[] = {pos_w, pos_src, nchild, chain, done, next, err, tiles};
+  void *ps[] = {pos_w, pos_src, hld, htop, hpos, seg_off, seg_top, seg_pos, done, next, err, tiles};
   for (void *p : ps) cudaFree(p);
-  pos_w = pos_src = nchild = chain = done = next = err = tiles = nullptr;
+  pos_w = pos_src = hld = htop = hpos = seg_top = seg_pos = done = next = err = tiles = nullptr;
+  seg_off = nullptr;
 }
 
 // Tiles in forest BFS order (level l of every graph, then level l + 1): a
@@ -589,7 +637,7 @@ void FillPlan::build_tiles(const TilePolicy &pol) {
   }
   GH_CUDA(cudaMemcpy(tiles, host.data(), sizeof(int) * need, cudaMemcpyHostToDevice));
   const int smem_dyn = enable_max_dynamic_smem(fill_flow_kernel);
-  smem = (size_t)max_u * 16 + (size_t)max_c * 8;
+  smem = (size_t)max_u * 16 + (size_t)std::max(max_segs, 1) * 8;
   GH_CHECK(smem <= (size_t)smem_dyn, H2H_ERR_DEVICE, "separator or tree too large for the fill staging");
   int per_sm = 0;
   GH_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fill_flow_kernel, threads, smem));
@@ -620,20 +668,22 @@ void FillPlan::enqueue(cudaStream_t s, const int64_t *slot_off, const int *slot_
   A.node_cnt = done + N;
   A.father = father;
   A.depth = depth;
-  A.nchild = nchild;
   A.drow = drow;
   A.dis = dis;
   A.pos_hash = pos_hash;
   A.pos_id = pos_id;
   A.pos_pos = pos_pos;
   A.pos_w = pos_w;
-  A.chain = chain;
+  A.hld = hld;
+  A.seg_off = seg_off;
+  A.seg_top = seg_top;
+  A.seg_pos = seg_pos;
   A.done = done;
   A.next = next;
   A.err = err;
   A.spin_limit = spin_limit_cycles();
   A.max_u = max_u;
-  A.max_c = max_c;
+  A.max_segs = std::max(max_segs, 1);
   if (fill_ev) GH_CUDA(cudaEventRecord(fill_ev[0], s));
   fill_flow_kernel<<<blocks, threads, smem, s>>>(A);
   GH_CUDA(cudaGetLastError());

@@ -142,6 +142,47 @@ void allocate_labels_and_bfs(Graph &g) {
     }
     if (g.tree_bfs.size() > end) g.tree_hash.push_back((int)g.tree_bfs.size());
   }
+  // heavy paths: subtree sizes bottom-up over the level order, heavy child
+  // = largest subtree (first in Childs order on ties), paths laid out by a
+  // depth-first walk that continues along the heavy child
+  std::vector<int> size(n, 1), heavy(n, -1), top(n, -1), hpos(n, -1);
+  for (int i = n - 1; i > 0; i--) size[g.father[g.tree_bfs[i]]] += size[g.tree_bfs[i]];
+  for (int v = 0; v < n; v++) {
+    int best = 0;
+    for (int k = g.child_off[v]; k < g.child_off[v + 1]; k++)
+      if (size[g.childs[k]] > best) { best = size[g.childs[k]]; heavy[v] = g.childs[k]; }
+  }
+  g.hld.assign(n, -1);
+  int next = 0;
+  std::vector<int> starts{g.head};
+  while (!starts.empty()) {
+    const int t = starts.back();
+    starts.pop_back();
+    for (int v = t; v >= 0; v = heavy[v]) {
+      top[v] = t;
+      hpos[v] = next;
+      g.hld[next++] = v;
+      for (int k = g.child_off[v + 1] - 1; k >= g.child_off[v]; k--)
+        if (g.childs[k] != heavy[v]) starts.push_back(g.childs[k]);
+    }
+  }
+  GH_CHECK(next == n, H2H_ERR_STATE, "heavy-path layout does not cover the tree");
+  // root-path segments per node: one more than the father's when the node
+  // starts a heavy path (counted top-down over the level order); the
+  // segment lists themselves are written on the GPU
+  std::vector<int> segs(n, 0);
+  for (int i = 0; i < n; i++) {
+    const int v = g.tree_bfs[i], f = g.father[v];
+    segs[v] = (f < 0 ? 0 : segs[f]) + (top[v] == v ? 1 : 0);
+  }
+  g.seg_off.assign(n + 1, 0);
+  g.max_segs = 0;
+  for (int v = 0; v < n; v++) {
+    g.seg_off[v + 1] = g.seg_off[v] + segs[v];
+    g.max_segs = std::max(g.max_segs, segs[v]);
+  }
+  g.htop.swap(top);
+  g.hpos.swap(hpos);
   g.t.bfs = clk.us();
 }
 
