@@ -219,8 +219,10 @@ void allocate_labels_and_bfs(Graph &g);                // tree.cpp
 void fill_labels_gpu(Graph &g);                        // labels.cu
 void download_labels(const Graph &g, int *dis_out);    // labels.cu, reference layout
 void upload_query_index(Graph &g);                     // query.cu
-void run_query_batch(const Graph &g, const int *x, const int *y, int *out, int64_t n, int mode,
-                     cudaStream_t s);                  // query.cu
+// query.cu; bad: the flag word set when a pair holds an id out of range
+// (nullptr: the graph's own)
+void run_query_batch(const Graph &g, const int *x, const int *y, int *out, int64_t n, int mode, cudaStream_t s,
+                     int *bad = nullptr);
 void run_query_batch_plain(const Graph &g, const int *x, const int *y, int *out, int64_t n, int mode,
                            cudaStream_t s);                  // query.cu, one thread per query
 

@@ -303,10 +303,12 @@ void upload_query_index(Graph &g) {
   GH_CHECK(g.dev.first && g.dev.rmq_hash && g.dev.rmq_id, H2H_ERR_STATE, "sparse table not built");
 }
 
-void run_query_batch(const Graph &g, const int *x, const int *y, int *out, int64_t n, int mode, cudaStream_t s) {
+void run_query_batch(const Graph &g, const int *x, const int *y, int *out, int64_t n, int mode, cudaStream_t s,
+                     int *bad) {
   if (n <= 0) return;
   const DeviceIndex &D = g.dev;
-  QArgs A{x, y, out, n, g.n, D.first, D.depth, D.rmq_hash, D.rmq_id, D.pos_hash, D.pos_pos, D.drow, D.dis, D.err};
+  QArgs A{x, y, out, n, g.n, D.first, D.depth, D.rmq_hash, D.rmq_id, D.pos_hash, D.pos_pos, D.drow, D.dis,
+          bad ? bad : D.err};
   static int nsm = 0;
   if (!nsm) {
     int dev = 0;

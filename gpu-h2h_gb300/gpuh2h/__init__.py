@@ -48,6 +48,17 @@ class _BatchInfo(C.Structure):
                                           "t_rebuild_us", "t_rebuild_fill_us")]
 
 
+class ServerConfig(C.Structure):
+    _fields_ = [("slots", C.c_int32), ("poll_us", C.c_int32), ("slot_pairs", C.c_int64),
+                ("memory_budget", C.c_int64)]
+
+
+class _ServerStats(C.Structure):
+    _fields_ = [(f, C.c_int64) for f in ("requests", "pairs", "batches", "max_inflight", "pending")] + \
+               [("kernel_us", C.c_double), ("span_us", C.c_double), ("admitted_bytes", C.c_int64),
+                ("memory_budget", C.c_int64)]
+
+
 class GenParams(C.Structure):
     _fields_ = [("n", C.c_int64), ("cols", C.c_int32), ("aspect_milli", C.c_int32), ("jitter_milli", C.c_int32),
                 ("drop_permille", C.c_int32), ("target_arcs", C.c_int64), ("diag_permille", C.c_int32),
@@ -97,6 +108,17 @@ SIGNATURES = {
     "h2h_batch_tune": (_i32, [_vp, _i32, _vp, _i32]),
     "h2h_batch_get_info": (_i32, [_vp, C.POINTER(_BatchInfo)]),
     "h2h_batch_free": (None, [_vp]),
+    "h2h_server_default_config": (None, [C.POINTER(ServerConfig)]),
+    "h2h_server_create": (_i32, [C.POINTER(ServerConfig), C.POINTER(_vp)]),
+    "h2h_server_add_graph": (_i32, [_vp, _vp, C.POINTER(_i32)]),
+    "h2h_server_remove_graph": (_i32, [_vp, _i32]),
+    "h2h_server_submit": (_i32, [_vp, _i32, _vp, _vp, _vp, _i64, _i32, C.POINTER(C.c_uint64)]),
+    "h2h_server_wait": (_i32, [_vp, C.c_uint64, _i64]),
+    "h2h_server_test": (_i32, [_vp, C.c_uint64]),
+    "h2h_server_release": (_i32, [_vp, C.c_uint64, C.POINTER(C.c_double)]),
+    "h2h_server_get_stats": (_i32, [_vp, C.POINTER(_ServerStats)]),
+    "h2h_server_reset_stats": (_i32, [_vp]),
+    "h2h_server_free": (None, [_vp]),
 }
 
 _lib = None
@@ -380,6 +402,80 @@ class Batch:
         buf = C.create_string_buffer(512)
         _check(self._L.h2h_batch_tune(self.b, rounds, C.cast(buf, C.c_void_p), 512))
         return buf.value.decode()
+
+
+class Server:
+    """Continuous-batching query server over resident graphs (h2h_server_*).
+
+    Server(slots=4, slot_pairs=1 << 20); add(graph) -> id; submit(id, x, y,
+    out) -> request (x, y, out: int32 numpy arrays kept alive until release);
+    wait(request); release(request) -> latency in us.
+    """
+
+    def __init__(self, slots: int = 4, slot_pairs: int = 1 << 20, poll_us: int = 5, memory_budget: int = 0):
+        _require_gpu()
+        L = load_library()
+        self._L = L
+        c = ServerConfig()
+        L.h2h_server_default_config(C.byref(c))
+        c.slots, c.slot_pairs, c.poll_us, c.memory_budget = slots, slot_pairs, poll_us, memory_budget
+        s = C.c_void_p()
+        _check(L.h2h_server_create(C.byref(c), C.byref(s)))
+        self.s = s
+        self._graphs = []
+        self._live = {}
+
+    def close(self):
+        if getattr(self, "s", None):
+            self._L.h2h_server_free(self.s)
+            self.s = None
+            self._live.clear()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def add(self, graph: "Graph") -> int:
+        gid = C.c_int()
+        _check(self._L.h2h_server_add_graph(self.s, graph.h, C.byref(gid)))
+        self._graphs.append(graph)
+        return gid.value
+
+    def remove(self, gid: int):
+        _check(self._L.h2h_server_remove_graph(self.s, gid))
+
+    def submit(self, gid: int, x: np.ndarray, y: np.ndarray, out: np.ndarray, mode: int = QUERY_LCA) -> int:
+        for a in (x, y, out):
+            assert a.dtype == np.int32 and a.flags.c_contiguous
+        rid = C.c_uint64()
+        _check(self._L.h2h_server_submit(self.s, gid, _p(x), _p(y), _p(out), len(x), mode, C.byref(rid)))
+        self._live[rid.value] = (x, y, out)
+        return rid.value
+
+    def wait(self, rid: int, timeout_us: int = -1):
+        _check(self._L.h2h_server_wait(self.s, rid, timeout_us))
+
+    def done(self, rid: int) -> bool:
+        r = self._L.h2h_server_test(self.s, rid)
+        if r < 0:
+            _check(r)
+        return r == 1
+
+    def release(self, rid: int) -> float:
+        lat = C.c_double()
+        _check(self._L.h2h_server_release(self.s, rid, C.byref(lat)))
+        self._live.pop(rid, None)
+        return lat.value
+
+    def stats(self) -> dict:
+        st = _ServerStats()
+        _check(self._L.h2h_server_get_stats(self.s, C.byref(st)))
+        return {f: getattr(st, f) for f, _ in _ServerStats._fields_}
+
+    def reset_stats(self):
+        _check(self._L.h2h_server_reset_stats(self.s))
 
 
 def gen_params(**kw) -> GenParams:

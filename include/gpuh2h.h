@@ -202,6 +202,56 @@ int h2h_batch_tune(h2h_batch *b, int rounds, char *policy_out, int cap);
 int h2h_batch_get_info(const h2h_batch *b, h2h_batch_info *info);
 void h2h_batch_free(h2h_batch *b);
 
+/* ---- Query server with continuous batching.  No counterpart in the
+ * reference, whose Query_noHub flow (main.cu:218-240) runs one prepared
+ * batch of one graph at a time.  Built graphs stay resident; requests
+ * (host buffers of pairs for one graph, one mode) are queued from any thread
+ * and answered asynchronously by a worker that keeps `slots` device batches
+ * in flight on separate streams and refills a slot from the queue as soon as
+ * it retires, joining requests of the same graph and mode (a request larger
+ * than a slot spans several).  Page-locked request buffers are transferred
+ * directly; pageable ones go through the slot's page-locked staging.  Pairs
+ * with a vertex id out of range answer -1.  Graphs must outlive the server
+ * (or be removed first). */
+typedef struct h2h_server h2h_server;
+
+typedef struct {
+  int32_t slots;          /* device batches in flight, one stream each      */
+  int32_t poll_us;        /* worker's event poll period while batches run   */
+  int64_t slot_pairs;     /* capacity of one batch, in pairs                */
+  int64_t memory_budget;  /* resident index bytes the server admits (<= 0:
+                             the free device memory at creation)            */
+} h2h_server_config;
+
+typedef struct {
+  int64_t requests, pairs, batches, max_inflight, pending;
+  double kernel_us;       /* summed device time of the query kernels        */
+  double span_us;         /* first submit to last answer since the last reset */
+  int64_t admitted_bytes, memory_budget;
+} h2h_server_stats;
+
+void h2h_server_default_config(h2h_server_config *c);
+int h2h_server_create(const h2h_server_config *c, h2h_server **out);
+/* Admits a labelled graph if its resident index fits the remaining budget
+ * (H2H_ERR_NOMEM otherwise). */
+int h2h_server_add_graph(h2h_server *s, h2h_graph *g, int *graph_id);
+/* Waits for the graph's requests, then frees its share of the budget. */
+int h2h_server_remove_graph(h2h_server *s, int graph_id);
+/* Queues n pairs; out receives the distances.  The buffers must stay valid
+ * until the request finishes. */
+int h2h_server_submit(h2h_server *s, int graph_id, const int *x, const int *y, int *out, int64_t n, int mode,
+                      uint64_t *request);
+/* Waits up to timeout_us (< 0: no limit) for a request (H2H_ERR_STATE on
+ * timeout); h2h_server_test returns 1 when finished, 0 when not. */
+int h2h_server_wait(h2h_server *s, uint64_t request, int64_t timeout_us);
+int h2h_server_test(h2h_server *s, uint64_t request);
+/* Forgets a finished request, returning its submit-to-answer latency. */
+int h2h_server_release(h2h_server *s, uint64_t request, double *latency_us);
+int h2h_server_get_stats(h2h_server *s, h2h_server_stats *st);
+int h2h_server_reset_stats(h2h_server *s);
+/* Drains the queue, then stops the worker and frees the slots. */
+void h2h_server_free(h2h_server *s);
+
 /* The stored arcs of a loaded graph in CSR order (self-loops dropped,
  * parallel arcs kept, each vertex's arcs in Edge-file order):
  * adj_off[n+1], adj_v[m], adj_w[m]. */
