@@ -125,6 +125,108 @@ def batched_build(threads: int, count: int) -> dict:
     return out
 
 
+SERVE_BIG = dict(name="road6m", n=6262104, target_arcs=15248146, aspect_milli=1500, jitter_milli=300,
+                 diag_permille=50, hw_tiers=1, hw_permille10=50, hw_k=3, hw_scale_milli=400, partition_height=15,
+                 seed=4, cols=0, drop_permille=0)
+
+
+def run_serving(args) -> int:
+    """Serving: the 6,262,104-vertex road graph (1:1.5 box, partition height
+    15) resident with 8 road graphs of 50k-1M vertices in one continuous-
+    batching server; Poisson request streams (1-10^5 pairs per request,
+    log-uniform, random graph) at 10^3-10^5 requests/s, latency of 10^5-pair
+    requests on the large graph, and closed-loop throughput against the HBM
+    roofline of the query kernel."""
+    import torch
+
+    import gpuh2h
+    world, rank, local = dist_setup()
+    torch.cuda.set_device(local)
+    threads = max(1, os.cpu_count() or 1)
+    root = tempfile.mkdtemp(prefix="h2h_serve_")
+    specs = [(SERVE_BIG["name"], {k: v for k, v in SERVE_BIG.items() if k != "name"})]
+    for i, p in enumerate(gpuh2h.road_batch_params(8, 50_000, 1_000_000, seed=23)):
+        specs.append(("res%d" % i, p))
+    graphs, build = [], []
+    for name, p in specs:
+        t0 = time.perf_counter()
+        arcs = gpuh2h.generate_road(root, name, **p)
+        t_gen = time.perf_counter() - t0
+        g, bt = build_index(gpuh2h.files_for(root, name), threads, H=p["partition_height"], C=2)
+        i = g.info()
+        build.append({"graph": name, "vertices": i["n"], "arcs": arcs, "partition_height": p["partition_height"],
+                      "build_s": bt, "gen_s": t_gen, "tree_height": i["tree_height"],
+                      "label_entries": i["label_size"], "device_gb": i["device_bytes"] / 1e9,
+                      "phases_ms": {k[2:-3]: i[k] / 1e3 for k in i if k.startswith("t_") and k.endswith("_us")}})
+        log("built %s: %d vertices, %.1f s, %.1f GB" % (name, i["n"], bt, i["device_bytes"] / 1e9))
+        graphs.append(g)
+    nv = [g.info()["n"] for g in graphs]
+    srv = gpuh2h.Server(slots=args.serve_slots, slot_pairs=1 << 17)
+    gids = [srv.add(g) for g in graphs]
+    # parity: server answers equal the direct batch API on every graph
+    for k, g in enumerate(graphs):
+        x, y = gpuh2h.uniform_pairs(nv[k], 50_000, 900 + k)
+        out = np.zeros(len(x), np.int32)
+        r = srv.submit(gids[k], x, y, out)
+        srv.wait(r)
+        srv.release(r)
+        assert np.array_equal(out, g.query(x, y)), "server answers differ on graph %d" % k
+    pct = lambda v, q: float(np.percentile(np.asarray(v), q))
+    runs = {}
+    # 10^5-pair requests on the large graph: alone, and four in flight
+    for inflight in (1, 4):
+        srv.reset_stats()
+        r = srv.load([gids[0]], [nv[0]], rate=0, size_lo=100_000, size_hi=100_000, requests=300,
+                     inflight=inflight, seed=31 + inflight)
+        st = srv.stats()
+        runs["big_1e5_inflight%d" % inflight] = {
+            "requests": r["requests"], "p50_us": pct(r["latency_us"], 50), "p99_us": pct(r["latency_us"], 99),
+            "queries_per_s": r["pairs"] / r["wall_s"], "kernel_us_per_batch": st["kernel_us"] / max(1, st["batches"])}
+    # open-loop Poisson streams over all graphs
+    for rate in (1e3, 1e4, 1e5):
+        srv.reset_stats()
+        r = srv.load(gids, nv, rate=rate, duration_s=args.serve_seconds, size_lo=1, size_hi=100_000, seed=int(rate))
+        st = srv.stats()
+        runs["poisson_%d" % int(rate)] = {
+            "requests": r["requests"], "pairs": r["pairs"], "late_submissions": r["late"],
+            "p50_us": pct(r["latency_us"], 50), "p99_us": pct(r["latency_us"], 99),
+            "p99_us_1e5_pair_requests": pct(r["latency_us"][r["sizes"] >= 50_000], 99)
+            if np.any(r["sizes"] >= 50_000) else None,
+            "queries_per_s": r["pairs"] / r["wall_s"], "batches": st["batches"], "max_inflight": st["max_inflight"]}
+    # saturation: closed loop on the large graph
+    srv.reset_stats()
+    r = srv.load([gids[0]], [nv[0]], rate=0, size_lo=100_000, size_hi=100_000, requests=600, inflight=16, seed=77)
+    st = srv.stats()
+    xs, ys = gpuh2h.uniform_pairs(nv[0], 200_000, 4242)
+    b_q = algorithmic_bytes(graphs[0], xs, ys) / len(xs)
+    try:
+        peak = float(json.load(open(os.path.join(REPO, "MEASURED_PEAKS.json")))["hbm_gbs"])
+        peak_src = "measured"
+    except Exception:
+        peak, peak_src = 6800.0, "fallback"
+    sat_q = r["pairs"] / r["wall_s"]
+    kern_q = r["pairs"] / (st["kernel_us"] / 1e6)
+    runs["saturation"] = {"requests": r["requests"], "queries_per_s": sat_q, "p50_us": pct(r["latency_us"], 50),
+                          "p99_us": pct(r["latency_us"], 99), "algorithmic_bytes_per_query": b_q,
+                          "served_frac_of_hbm": sat_q * b_q / 1e9 / peak,
+                          "kernel_queries_per_s": kern_q, "kernel_frac_of_hbm": kern_q * b_q / 1e9 / peak,
+                          "peak_gbs": peak, "peak_source": peak_src}
+    line = {"metric": "served queries/s and p50/p99 latency (continuous batching, resident graphs)",
+            "impl": "ours", "unit": "queries/s", "value": sat_q, "n_gpus": 1, "higher_is_better": True,
+            "dtype": "int32", "data": "synthetic",
+            "config": {"workload": "road6m: 6,262,104 vertices (1:1.5 box, partition height 15, C=2) + 8 resident "
+                                   "road graphs of 50k-1M vertices; requests of 1-1e5 pairs (log-uniform) to "
+                                   "random graphs", "slots": args.serve_slots, "slot_pairs": 1 << 17},
+            "build": build, "runs": runs,
+            "parity": "server answers to 5e4 pairs per graph equal h2h_query_batch_host"}
+    print(json.dumps(line), flush=True)
+    srv.close()
+    for g in graphs:
+        g.close()
+    shutil.rmtree(root, ignore_errors=True)
+    return 0
+
+
 def query_pairs(g, n_vertices: int, seed: int):
     import gpuh2h
     x, y = gpuh2h.uniform_pairs(n_vertices, Q_UNIFORM, seed)
@@ -239,7 +341,7 @@ def barrier(world: int):
         dist.barrier()
 
 
-def build_index(files, threads: int):
+def build_index(files, threads: int, H: int = H, C: int = C):
     import gpuh2h
     t0 = time.perf_counter()
     g = gpuh2h.Graph(WORKLOAD["name"], H, C, threads, 1, files=files)
@@ -325,10 +427,15 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=10.0, help="seconds of CPU query work for cpu_baseline")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--batch-graphs", type=int, default=64, help="graphs of the batched-build measurement (0: skip)")
+    ap.add_argument("--serve", action="store_true", help="run the serving measurement instead")
+    ap.add_argument("--serve-slots", type=int, default=4)
+    ap.add_argument("--serve-seconds", type=float, default=2.0)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
         return run_reference_arm(args)
+    if args.serve:
+        return run_serving(args)
 
     import torch
     world, rank, local = dist_setup()

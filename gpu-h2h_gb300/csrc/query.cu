@@ -83,22 +83,24 @@ __global__ void query_kernel(QArgs A) {
   }
 }
 
-// Warp-tiled batch: a warp owns 32 consecutive queries.  Phase 1: every lane
-// resolves its own query (ids, LCA through the sparse table, row bases, the
-// position range) -- 32 independent dependent-load chains in flight.  Phase
-// 2: the whole warp walks each query's positions in turn with 4-way unrolled
-// loads (position, then the two label entries) and a warp min
-// (__reduce_min_sync); the owning lane keeps the answer and the 32 answers
-// leave in one coalesced store.
-template <bool LCA_MODE>
+// Warp-tiled batch: a warp owns TILE consecutive queries.  Phase 1: lane i
+// < TILE resolves query i (ids, LCA through the sparse table, row bases, the
+// position range) -- TILE independent dependent-load chains in flight.
+// Phase 2: the whole warp walks each query's positions in turn with 4-way
+// unrolled loads (position, then the two label entries) and a warp min
+// (__reduce_min_sync); the owning lane keeps the answer and the answers
+// leave in one coalesced store.  TILE = 32 for large batches; a batch too
+// small to fill the GPU's resident warps takes a narrower tile, so more
+// warps share its walks and the batch finishes sooner.
+template <bool LCA_MODE, int TILE>
 __global__ void __launch_bounds__(256, 8) query_tile_kernel(QArgs A) {
   const int lane = threadIdx.x & 31;
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  for (int64_t tile = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; (tile << 5) < A.n; tile += nwarps) {
-    const int64_t q = (tile << 5) + lane;
+  for (int64_t tile = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; tile * TILE < A.n; tile += nwarps) {
+    const int64_t q = tile * TILE + lane;
     int res = INT_MAX, len = 0;
     int64_t pb = 0, bx = 0, by = 0;
-    if (q < A.n) {
+    if (lane < TILE && q < A.n) {
       const int a = __ldg(A.x + q), b = __ldg(A.y + q);
       const bool valid = (unsigned)a < (unsigned)A.nv && (unsigned)b < (unsigned)A.nv;
       if (!valid) {
@@ -124,7 +126,8 @@ __global__ void __launch_bounds__(256, 8) query_tile_kernel(QArgs A) {
         }
       }
     }
-    for (int s = 0; s < 32; s++) {
+#pragma unroll 1
+    for (int s = 0; s < TILE; s++) {
       const int L = __shfl_sync(0xffffffffu, len, s);
       if (L == 0) continue;
       const int64_t PB = __shfl_sync(0xffffffffu, pb, s);
@@ -153,7 +156,7 @@ __global__ void __launch_bounds__(256, 8) query_tile_kernel(QArgs A) {
       m = __reduce_min_sync(0xffffffffu, m);
       if (lane == s) res = m;
     }
-    if (q < A.n) A.out[q] = res;
+    if (lane < TILE && q < A.n) A.out[q] = res;
   }
 }
 
@@ -316,18 +319,29 @@ void run_query_batch(const Graph &g, const int *x, const int *y, int *out, int64
     GH_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
   }
   const int threads = 256;
-  const int64_t tiles = (n + 31) / 32;
-  static int per_sm[2] = {0, 0};  // resident 256-thread blocks per SM, LCA / noLCA kernels
   const int mi = mode == H2H_QUERY_LCA ? 0 : 1;
+  using Kernel = void (*)(QArgs);
+  static const Kernel kernels[2][4] = {
+      {query_tile_kernel<true, 32>, query_tile_kernel<true, 16>, query_tile_kernel<true, 8>,
+       query_tile_kernel<true, 4>},
+      {query_tile_kernel<false, 32>, query_tile_kernel<false, 16>, query_tile_kernel<false, 8>,
+       query_tile_kernel<false, 4>}};
+  static int per_sm[2] = {0, 0};  // resident 256-thread blocks per SM (all tile widths use 32 registers)
   if (!per_sm[mi]) {
-    GH_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-        &per_sm[mi], mode == H2H_QUERY_LCA ? query_tile_kernel<true> : query_tile_kernel<false>, threads, 0));
+    GH_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm[mi], kernels[mi][0], threads, 0));
     per_sm[mi] = std::max(1, per_sm[mi]);
   }
+  // narrowest tile whose warps still fit one wave of resident warps
+  const int64_t resident_warps = (int64_t)nsm * per_sm[mi] * (threads / 32);
+  int ti = 0, tile = 32;
+  while (ti < 3 && ((n + tile / 2 - 1) / (tile / 2)) <= resident_warps) {
+    tile /= 2;
+    ti++;
+  }
+  const int64_t tiles = (n + tile - 1) / tile;
   // one wave of resident blocks, grid-striding over the tiles
   const int blocks = (int)std::min<int64_t>((tiles + 7) / 8, (int64_t)nsm * per_sm[mi]);
-  if (mode == H2H_QUERY_LCA) query_tile_kernel<true><<<std::max(1, blocks), threads, 0, s>>>(A);
-  else query_tile_kernel<false><<<std::max(1, blocks), threads, 0, s>>>(A);
+  kernels[mi][ti]<<<std::max(1, blocks), threads, 0, s>>>(A);
   GH_CUDA(cudaGetLastError());
 }
 

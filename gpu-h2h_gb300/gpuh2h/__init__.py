@@ -59,6 +59,15 @@ class _ServerStats(C.Structure):
                 ("memory_budget", C.c_int64)]
 
 
+class LoadParams(C.Structure):
+    _fields_ = [("rate", C.c_double), ("duration_s", C.c_double), ("size_lo", C.c_int64), ("size_hi", C.c_int64),
+                ("requests", C.c_int64), ("inflight", C.c_int32), ("mode", C.c_int32), ("seed", C.c_uint64)]
+
+
+class _LoadResult(C.Structure):
+    _fields_ = [("requests", C.c_int64), ("pairs", C.c_int64), ("late", C.c_int64), ("wall_s", C.c_double)]
+
+
 class GenParams(C.Structure):
     _fields_ = [("n", C.c_int64), ("cols", C.c_int32), ("aspect_milli", C.c_int32), ("jitter_milli", C.c_int32),
                 ("drop_permille", C.c_int32), ("target_arcs", C.c_int64), ("diag_permille", C.c_int32),
@@ -119,6 +128,8 @@ SIGNATURES = {
     "h2h_server_get_stats": (_i32, [_vp, C.POINTER(_ServerStats)]),
     "h2h_server_reset_stats": (_i32, [_vp]),
     "h2h_server_free": (None, [_vp]),
+    "h2h_server_load": (_i32, [_vp, _vp, _vp, _i32, C.POINTER(LoadParams), _vp, _vp, _vp, _i64,
+                               C.POINTER(_LoadResult)]),
 }
 
 _lib = None
@@ -476,6 +487,24 @@ class Server:
 
     def reset_stats(self):
         _check(self._L.h2h_server_reset_stats(self.s))
+
+    def load(self, gids, n_vertices, rate: float = 0.0, duration_s: float = 1.0, size_lo: int = 1,
+             size_hi: int = 100_000, requests: int = 0, inflight: int = 1, mode: int = QUERY_LCA, seed: int = 1,
+             max_requests: int = 1_000_000) -> dict:
+        """Drive the server with h2h_server_load; returns per-request latency
+        (us, from scheduled arrival), sizes and graph indices."""
+        g = np.ascontiguousarray(gids, np.int32)
+        nv = np.ascontiguousarray(n_vertices, np.int32)
+        p = LoadParams(rate, duration_s, size_lo, size_hi, requests, inflight, mode, seed)
+        lat = np.zeros(max_requests, np.float64)
+        sz = np.zeros(max_requests, np.int64)
+        go = np.zeros(max_requests, np.int32)
+        r = _LoadResult()
+        _check(self._L.h2h_server_load(self.s, _p(g), _p(nv), len(g), C.byref(p), _p(lat), _p(sz), _p(go),
+                                       max_requests, C.byref(r)))
+        k = min(r.requests, max_requests)
+        return dict(requests=r.requests, pairs=r.pairs, late=r.late, wall_s=r.wall_s, latency_us=lat[:k],
+                    sizes=sz[:k], graph=go[:k])
 
 
 def gen_params(**kw) -> GenParams:

@@ -55,6 +55,32 @@ int h2h_gen_local_pairs(const h2h_graph *g, int64_t n, int max_hops, uint64_t se
 int h2h_query_batch_plain(const h2h_graph *g, const int *x_dev, const int *y_dev, int *out_dev, int64_t n,
                           int mode, void *stream);
 
+/* Load generator for a query server (measurement tool).  Each request goes
+ * to a uniformly drawn graph of graph_ids (vertex counts graph_n) with a
+ * size drawn log-uniform in [size_lo, size_hi] pairs of uniform vertices.
+ * rate > 0: open loop, Poisson arrivals at `rate` per second for duration_s;
+ * a request's latency counts from its scheduled arrival, so a generator
+ * that falls behind does not hide queueing.  rate <= 0: closed loop,
+ * `inflight` requests outstanding until `requests` have finished.  Pairs are
+ * drawn beforehand into page-locked pools; answers land in a page-locked
+ * ring, one region per outstanding request. */
+typedef struct {
+  double rate, duration_s;
+  int64_t size_lo, size_hi, requests;
+  int32_t inflight, mode;
+  uint64_t seed;
+} h2h_load_params;
+
+typedef struct {
+  int64_t requests, pairs, late;  /* late: submissions more than 100 us behind schedule */
+  double wall_s;
+} h2h_load_result;
+
+/* latency_us / sizes / graph_of receive one entry per finished request, up
+ * to max_requests. */
+int h2h_server_load(h2h_server *s, const int *graph_ids, const int *graph_n, int ngraphs, const h2h_load_params *p,
+                    double *latency_us, int64_t *sizes, int *graph_of, int64_t max_requests, h2h_load_result *res);
+
 #ifdef __cplusplus
 }
 #endif
