@@ -146,7 +146,7 @@ int h2h_batch_build(h2h_graph *const *graphs, int count, int threads, h2h_batch 
     b->info.t_contract_us = event_us(b->ev[0], b->ev[1]);
     b->info.t_global_us = event_us(b->ev[1], b->ev[2]);
     clk.reset();
-    b->elim->download();
+    b->elim->build_lists();
     for (gh::Graph *g : b->gs) {
       g->contract_device = 1;
       g->t.td_gpu = 0;
@@ -178,12 +178,12 @@ int h2h_batch_build(h2h_graph *const *graphs, int count, int threads, h2h_batch 
     gh::TilePolicy pol;
     if (const char *e = std::getenv("GPUH2H_TILE_POLICY"))
       GH_CHECK(pol.parse(e), H2H_ERR_ARG, "GPUH2H_TILE_POLICY: expected 8 entries small_work/col_block/sep_chunk");
-    b->fill = std::make_unique<gh::FillPlan>(b->gs, pol);
+    b->fill = std::make_unique<gh::FillPlan>(b->gs, pol, b->elim->lists);
     GH_CUDA(cudaDeviceSynchronize());
     b->info.t_fill_plan_us = clk.us();
     clk.reset();
     cudaEvent_t fev[2] = {b->ev[0], b->ev[3]};
-    b->fill->enqueue(b->stream, b->elim->slot_off, b->elim->slot_w, fev);
+    b->fill->enqueue(b->stream, fev);
     b->fill->check_error();
     b->info.t_fill_us = event_us(b->ev[0], b->ev[3]);
     clk.reset();
@@ -218,7 +218,8 @@ int h2h_batch_rebuild(h2h_batch *b) {
       GH_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
       try {
         b->elim->enqueue(b->stream);
-        b->fill->enqueue(b->stream, b->elim->slot_off, b->elim->slot_w, nullptr);
+        b->elim->enqueue_gather(b->stream);
+        b->fill->enqueue(b->stream, nullptr);
       } catch (...) {
         cudaStreamEndCapture(b->stream, &graph);
         if (graph) cudaGraphDestroy(graph);
@@ -245,12 +246,8 @@ int h2h_batch_rebuild(h2h_batch *b) {
 int h2h_batch_sync_host(h2h_batch *b) {
   if (!b) { gh::set_last_error("null batch"); return H2H_ERR_ARG; }
   return gh::guarded([&] {
+    // the lists and position arrays are read from the device on demand
     GH_CUDA(cudaStreamSynchronize(b->stream));
-    b->elim->download(true);
-    for (gh::Graph *g : b->gs)
-      for (int v = 0; v < g->n; v++)
-        for (int64_t k = g->pos_hash[v]; k < g->pos_hash[v + 1]; k++)
-          g->pos_w[k] = g->pos_src[k] < 0 ? 0 : g->x_w[g->x_off[v] + g->pos_src[k]];
   });
 }
 

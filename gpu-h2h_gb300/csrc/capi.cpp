@@ -309,8 +309,16 @@ int h2h_copy_adj(const h2h_graph *h, int64_t *adj_hash, int *adj_id, int *adj_w)
     const gh::Graph &g = h->g;
     GH_CHECK(g.contracted, H2H_ERR_STATE, "not contracted");
     if (adj_hash) std::copy(g.x_off.begin(), g.x_off.end(), adj_hash);
-    if (adj_id) std::copy(g.x_id.begin(), g.x_id.end(), adj_id);
-    if (adj_w) std::copy(g.x_w.begin(), g.x_w.end(), adj_w);
+    if (adj_id || adj_w) {
+      gh::Graph &gm = const_cast<gh::Graph &>(g);
+      gh::download_lists(gm);  // the lists live on the device
+      if (adj_id) std::copy(g.x_id.begin(), g.x_id.end(), adj_id);
+      if (adj_w) std::copy(g.x_w.begin(), g.x_w.end(), adj_w);
+      if (g.label_mode != H2H_LABEL_L3) {
+        std::vector<int>().swap(gm.x_id);
+        std::vector<int>().swap(gm.x_w);
+      }
+    }
   });
 }
 
@@ -322,8 +330,7 @@ int h2h_copy_labels(const h2h_graph *h, int64_t *dis_hash, int *dis, int64_t *po
     if (dis_hash) std::copy(g.dis_hash.begin(), g.dis_hash.end(), dis_hash);
     if (dis) gh::download_labels(g, dis);
     if (pos_hash) std::copy(g.pos_hash.begin(), g.pos_hash.end(), pos_hash);
-    if (pos_id) std::copy(g.pos_id.begin(), g.pos_id.end(), pos_id);
-    if (pos_pos) std::copy(g.pos_pos.begin(), g.pos_pos.end(), pos_pos);
+    if (pos_id || pos_pos) gh::download_positions(g, pos_id, pos_pos);
   });
 }
 

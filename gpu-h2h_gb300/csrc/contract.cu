@@ -479,6 +479,41 @@ __global__ void gather_lists_kernel(const int64_t *slot_off, const int *lsize, c
   }
 }
 
+// rank[v] = position of v in the elimination order.
+__global__ void rank_kernel(const int *elim, int *rank, int n) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) rank[elim[i]] = i;
+}
+
+// father = the member of X(v) eliminated first (getTreeStructure,
+// TreeStructure.cu:431-473: min rank over v's upper neighbours; -1 for the
+// last vertex).  One warp per vertex; ranks are distinct.
+__global__ void father_kernel(const int64_t *off, const int *id, const int *rank, int *father, int n) {
+  const int lane = threadIdx.x & 31;
+  for (int64_t v = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; v < n;
+       v += (gridDim.x * (int64_t)blockDim.x) >> 5) {
+    int best = INT_MAX, bid = -1;
+    for (int64_t k = off[v] + lane; k < off[v + 1]; k += 32) {
+      const int a = id[k], r = rank[a];
+      if (r < best) { best = r; bid = a; }
+    }
+    const int m = __reduce_min_sync(0xffffffffu, best);
+    const unsigned who = __ballot_sync(0xffffffffu, best == m && bid >= 0);
+    const int f = who ? __shfl_sync(0xffffffffu, bid, __ffs(who) - 1) : -1;
+    if (lane == 0) father[v] = f;
+  }
+}
+
+// Device lists of a contraction (owned through ListStore::keep).
+struct ListArrays {
+  int64_t *off = nullptr;
+  int *id = nullptr, *w = nullptr;
+  ~ListArrays() {
+    cudaFree(off);
+    cudaFree(id);
+    cudaFree(w);
+  }
+};
+
 template <typename T>
 T *dalloc(size_t n) {
   T *p = nullptr;
@@ -837,6 +872,9 @@ void ElimPlan::release() {
                 elim_init, deg0, deg_init, h0, cpos, err, ljunk, cell_start, cell_count, adj_off, adj_v, adj_w,
                 heap_verts, pstage};
   for (void *p : ps) cudaFree(p);
+  cudaFree(rank);
+  cudaFree(father_dev);
+  rank = father_dev = nullptr;
   for (cudaStream_t st : side) cudaStreamDestroy(st);
   for (cudaEvent_t e : ev_join) cudaEventDestroy(e);
   if (ev_fork) cudaEventDestroy(ev_fork);
@@ -948,55 +986,72 @@ void ElimPlan::check_error() {
                              : "contraction: a list outgrew the staging bound");
 }
 
-void ElimPlan::download(bool weights_only) {
-  std::vector<int> f_lsize(N);
+void ElimPlan::build_lists() {
+  std::vector<int> f_lsize(N), f_elim(N), f_father(N);
   GH_CUDA(cudaMemcpy(f_lsize.data(), lsize, sizeof(int) * N, cudaMemcpyDeviceToHost));
-  std::vector<int64_t> out_off(N + 1, 0);
-  for (int v = 0; v < N; v++) out_off[v + 1] = out_off[v] + f_lsize[v];
-  const int64_t tot = out_off[N];
-  int64_t tmp_bytes = 0;
-  int64_t *d_out_off = nullptr;
-  int *d_out_nbr = nullptr, *d_out_w = nullptr;
-  try {
-    d_out_off = palloc<int64_t>(N + 1, tmp_bytes);
-    d_out_nbr = palloc<int>(std::max<int64_t>(tot, 1), tmp_bytes);
-    d_out_w = palloc<int>(std::max<int64_t>(tot, 1), tmp_bytes);
-    GH_CUDA(cudaMemcpy(d_out_off, out_off.data(), sizeof(int64_t) * (N + 1), cudaMemcpyHostToDevice));
-    gather_lists_kernel<<<std::max(1, std::min(8192, (N * 32 + 255) / 256)), 256>>>(
-        slot_off, lsize, d_out_off, slot_nbr, slot_w, d_out_nbr, d_out_w, N);
-    GH_CUDA(cudaGetLastError());
-    std::vector<int> f_nbr(weights_only ? 0 : tot), f_w(tot), f_elim(weights_only ? 0 : N);
-    if (!weights_only) {
-      GH_CUDA(cudaMemcpy(f_elim.data(), elim, sizeof(int) * N, cudaMemcpyDeviceToHost));
-      GH_CUDA(cudaMemcpy(f_nbr.data(), d_out_nbr, sizeof(int) * tot, cudaMemcpyDeviceToHost));
-    }
-    GH_CUDA(cudaMemcpy(f_w.data(), d_out_w, sizeof(int) * tot, cudaMemcpyDeviceToHost));
-    for (size_t i = 0; i < gs.size(); i++) {
-      Graph &g = *gs[i];
-      const int vb = vbase[i];
-      const int64_t ob = out_off[vb];
-      if (!weights_only) {
-        for (int v = 0; v < g.n; v++) g.elim[v] = f_elim[vb + v] - vb;
-        g.x_off.assign(g.n + 1, 0);
-        for (int v = 0; v < g.n; v++) g.x_off[v + 1] = g.x_off[v] + f_lsize[vb + v];
-        const int64_t t = g.x_off[g.n];
-        g.x_id.resize(t);
-        for (int64_t k = 0; k < t; k++) g.x_id[k] = f_nbr[ob + k] - vb;
-        g.decomposition_size = t + g.n;
-      }
-      g.x_w.assign(f_w.begin() + ob, f_w.begin() + ob + (out_off[vb + g.n] - ob));
-    }
-  } catch (...) {
-    cudaFree(d_out_off); cudaFree(d_out_nbr); cudaFree(d_out_w);
-    throw;
+  std::vector<int64_t> off(N + 1, 0);
+  for (int v = 0; v < N; v++) off[v + 1] = off[v] + f_lsize[v];
+  const int64_t tot = off[N];
+  auto la = std::make_shared<ListArrays>();
+  la->off = dalloc<int64_t>(N + 1);
+  la->id = dalloc<int>(std::max<int64_t>(tot, 1));
+  la->w = dalloc<int>(std::max<int64_t>(tot, 1));
+  lists.off = la->off;
+  lists.id = la->id;
+  lists.w = la->w;
+  lists.total = tot;
+  lists.keep = la;
+  if (!rank) rank = palloc<int>(N, bytes);
+  if (!father_dev) father_dev = palloc<int>(N, bytes);
+  GH_CUDA(cudaMemcpy(lists.off, off.data(), sizeof(int64_t) * (N + 1), cudaMemcpyHostToDevice));
+  enqueue_gather(0);
+  rank_kernel<<<std::max(1, std::min(4096, (N + 255) / 256)), 256>>>(elim, rank, N);
+  GH_CUDA(cudaGetLastError());
+  father_kernel<<<std::max(1, std::min(8192, (N * 32 + 255) / 256)), 256>>>(lists.off, lists.id, rank, father_dev, N);
+  GH_CUDA(cudaGetLastError());
+  GH_CUDA(cudaMemcpy(f_elim.data(), elim, sizeof(int) * N, cudaMemcpyDeviceToHost));
+  GH_CUDA(cudaMemcpy(f_father.data(), father_dev, sizeof(int) * N, cudaMemcpyDeviceToHost));
+  for (size_t i = 0; i < gs.size(); i++) {
+    Graph &g = *gs[i];
+    const int vb = vbase[i];
+    for (int v = 0; v < g.n; v++) g.elim[v] = f_elim[vb + v] - vb;
+    g.father.assign(g.n, -1);
+    for (int v = 0; v < g.n; v++) g.father[v] = f_father[vb + v] < 0 ? -1 : f_father[vb + v] - vb;
+    g.x_off.assign(g.n + 1, 0);
+    for (int v = 0; v < g.n; v++) g.x_off[v + 1] = g.x_off[v] + f_lsize[vb + v];
+    g.decomposition_size = g.x_off[g.n] + g.n;
+    std::vector<int>().swap(g.x_id);
+    std::vector<int>().swap(g.x_w);
+    g.dev.lists = lists;
+    g.dev.x_base = off[vb];
+    g.dev.id_base = vb;
   }
-  cudaFree(d_out_off); cudaFree(d_out_nbr); cudaFree(d_out_w);
+}
+
+void ElimPlan::enqueue_gather(cudaStream_t s) {
+  gather_lists_kernel<<<std::max(1, std::min(8192, (N * 32 + 255) / 256)), 256, 0, s>>>(
+      slot_off, lsize, lists.off, slot_nbr, slot_w, lists.id, lists.w, N);
+  GH_CUDA(cudaGetLastError());
+}
+
+void download_lists(Graph &g) {
+  const ListStore &L = g.dev.lists;
+  GH_CHECK(L.id && (int64_t)g.x_off.size() == g.n + 1, H2H_ERR_STATE, "not contracted");
+  const int64_t t = g.x_off[g.n];
+  g.x_id.resize(t);
+  g.x_w.resize(t);
+  if (t) {
+    GH_CUDA(cudaMemcpy(g.x_id.data(), L.id + g.dev.x_base, sizeof(int) * t, cudaMemcpyDeviceToHost));
+    GH_CUDA(cudaMemcpy(g.x_w.data(), L.w + g.dev.x_base, sizeof(int) * t, cudaMemcpyDeviceToHost));
+  }
+  if (g.dev.id_base)
+    for (int64_t k = 0; k < t; k++) g.x_id[k] -= g.dev.id_base;
 }
 
 // Whole elimination of one graph on the GPU: partition levels H..C+1, then
 // the global order over the vertices of levels <= C.  Fills g.elim
-// (elimination order), g.x_off / x_id / x_w (upper neighbours X(v)\{v}
-// sorted by id, the lists at elimination time) and g.gpu_vertices.
+// (elimination order), g.father, g.x_off and g.gpu_vertices; the lists
+// X(v)\{v} (sorted by id, the lists at elimination time) stay on the device.
 void contract_gpu(Graph &g) {
   Clock clk;
   const bool trace = std::getenv("GPUH2H_TRACE") != nullptr;
@@ -1024,7 +1079,7 @@ void contract_gpu(Graph &g) {
   g.t.td_gpu = clk.us() - heap_us;  // partition levels
   g.t.td_cpu = heap_us;             // global order over levels <= C (TDInCPUTime in the reference, on the GPU here)
   clk.reset();
-  plan.download();
+  plan.build_lists();
   g.t.translate_back = clk.us();
 }
 

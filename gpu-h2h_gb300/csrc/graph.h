@@ -11,6 +11,17 @@
 
 namespace gh {
 
+// X(v)\{v} lists after contraction, on the device, in the numbering of the
+// contraction that produced them (a batch's forest, or one graph): list of
+// vertex v is id[off[v] .. off[v+1]) (neighbour ids, sorted) with shortcut
+// weights w.  `keep` owns the arrays.
+struct ListStore {
+  int64_t *off = nullptr;
+  int *id = nullptr, *w = nullptr;
+  int64_t total = 0;
+  std::shared_ptr<void> keep;
+};
+
 // Device-resident index used by the label fill and the query kernels.
 // Label rows are padded so every row starts on a 16-byte boundary
 // (drow[v] is a multiple of 4 ints); the reference layout is restored on
@@ -33,6 +44,12 @@ struct DeviceIndex {
   int *dis = nullptr;         // padded labels          [dis_padded]
   int *father = nullptr;      // father                 [n]
   int *err = nullptr;         // kernel error word      [1]
+  // views into the contraction's device lists and the fill's position
+  // arrays: the graph's entries start at x_base / pos_base, its vertex ids
+  // at id_base (non-zero in a batch)
+  ListStore lists;
+  int64_t x_base = 0, pos_base = 0;
+  int id_base = 0;
   int64_t bytes = 0, rmq_bytes = 0;
   std::vector<void *> owned;      // label-side allocations of this handle
   std::vector<void *> owned_rmq;  // first, rmq_hash, rmq_id (built with the tree)
@@ -69,7 +86,7 @@ struct Graph {
   // contraction results
   std::vector<int> height;                  // CHInfo.second after the partition levels
   std::vector<int64_t> x_off;               // X(v)\{v}: upper neighbours, CSR by vertex [n+1]
-  std::vector<int> x_id, x_w;               //   sorted by id, shortcut weights
+  std::vector<int> x_id, x_w;               //   sorted by id, shortcut weights (host copies on demand)
   int gpu_vertices = 0;                     // vertexesConstructedInGPU
   int64_t decomposition_size = 0;           // size1 = sum(|X(v)|+1)
   bool contracted = false;
@@ -80,8 +97,9 @@ struct Graph {
   int64_t euler_n = 0, h2h_size = 0, rmq_total = 0;  // rmq_total: RMQ_ID entries (the table is on the GPU)
   // labels (H2HConsturction.cu), reference layout on the host
   std::vector<int64_t> dis_hash, pos_hash;
+  // host position lists: built for L3 labels only (L4 builds them on the GPU;
+  // accessors download them)
   std::vector<int> pos_id, pos_pos, pos_w;  // pos_w: shortcut weight per pos entry (0 for v itself)
-  std::vector<int> pos_src;                 // index of the pos entry in v's X list (-1 for v itself)
   std::vector<int64_t> drow_host;           // padded device row offsets (absolute in a batch's forest)
   std::vector<int> tree_bfs, tree_hash;     // TreeBFS / TreeHash
   // heavy-path decomposition of the tree for ancestor lookups in the fill:
@@ -132,6 +150,8 @@ struct ElimPlan {
   int *deg_init = nullptr, *elim_init = nullptr, *heap_verts = nullptr;
   int64_t *slot_off = nullptr, *slot_off_init = nullptr;
   unsigned long long *pool_next = nullptr, *pool_first = nullptr;
+  ListStore lists;       // compact final lists (forest numbering), after build_lists()
+  int *rank = nullptr, *father_dev = nullptr;
   int64_t bytes = 0;
   explicit ElimPlan(const std::vector<Graph *> &graphs);
   ~ElimPlan();
@@ -144,8 +164,13 @@ struct ElimPlan {
   void enqueue(cudaStream_t s, cudaEvent_t *heap_ev = nullptr, bool trace = false);
   void launch_one(const Launch &Lc, cudaStream_t s, bool trace);
   void check_error();  // synchronises; throws on a kernel error code
-  // Elimination order, X(v) lists and their weights back into each graph.
-  void download(bool weights_only = false);
+  // After the first enqueue: compact the final lists on the device, pick each
+  // vertex's father (min elimination rank over its list) there, and hand each
+  // graph its elimination order, list offsets and fathers; the lists stay on
+  // the device (each graph's DeviceIndex gets a view).
+  void build_lists();
+  // Refreshes the compact lists' entries from the slot arrays (replays).
+  void enqueue_gather(cudaStream_t s);
   void set_weights(int gi, const int *w, cudaStream_t s);  // arc weights in the graph's file order
 };
 
@@ -176,6 +201,7 @@ struct FillPlan {
   std::shared_ptr<void> storage;  // forest arrays shared with the graphs' views
   int64_t *drow = nullptr, *pos_hash = nullptr;
   int *pos_pos = nullptr, *pos_id = nullptr, *pos_w = nullptr, *pos_src = nullptr, *father = nullptr;
+  ListStore lists;
   int *depth = nullptr, *dis = nullptr;
   // workspace
   int *hld = nullptr, *htop = nullptr, *hpos = nullptr, *seg_top = nullptr, *seg_pos = nullptr;
@@ -186,16 +212,16 @@ struct FillPlan {
   size_t smem = 0;
   int nsm = 0;
   int64_t work_bytes = 0;
-  FillPlan(const std::vector<Graph *> &graphs, const TilePolicy &pol);
+  // lists: the graphs' X lists in the same forest numbering.
+  FillPlan(const std::vector<Graph *> &graphs, const TilePolicy &pol, const ListStore &lists);
   ~FillPlan();
   void release_work();
   FillPlan(const FillPlan &) = delete;
   FillPlan &operator=(const FillPlan &) = delete;
   void build_tiles(const TilePolicy &pol);
-  // Resets rows and flags and runs the fill on s.  With slot arrays given,
-  // the shortcut weights are first gathered from the contraction's lists
-  // (ElimPlan numbering must match); otherwise the uploaded pos_w is used.
-  void enqueue(cudaStream_t s, const int64_t *slot_off, const int *slot_w, cudaEvent_t *fill_ev = nullptr);
+  // Gathers the shortcut weights of the pos entries from the lists, resets
+  // rows and flags and runs the fill on s.
+  void enqueue(cudaStream_t s, cudaEvent_t *fill_ev = nullptr);
   void check_error();            // synchronises; throws if a dependency wait ran out
   void attach(bool first);       // per-graph views, max_label; first: also drow_host
 };
@@ -218,6 +244,10 @@ inline void build_tree_and_rmq(Graph &g) {
 void allocate_labels_and_bfs(Graph &g);                // tree.cpp
 void fill_labels_gpu(Graph &g);                        // labels.cu
 void download_labels(const Graph &g, int *dis_out);    // labels.cu, reference layout
+// labels.cu: the graph's position lists (reference layout, graph-local ids)
+void download_positions(const Graph &g, int *pos_id, int *pos_pos);
+// contract.cu: host copies of the X lists (graph-local ids) from the device
+void download_lists(Graph &g);
 void upload_query_index(Graph &g);                     // query.cu
 // query.cu; bad: the flag word set when a pair holds an id out of range
 // (nullptr: the graph's own)

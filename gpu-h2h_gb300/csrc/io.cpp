@@ -191,7 +191,8 @@ static std::string construct_row(const Graph &g, bool after_labels) {
   double rmq_mb = 0, label_mb;
   if (after_labels) {                                  // mallocH2HLabel_noHub, H2HConsturction.cu:704-707
     rmq_mb = ((double)g.euler_n * 8 + (double)g.rmq_total * 4 + (double)g.n * 4) / MB;
-    label_mb = ((double)(g.n + 1) * 8 * 2 + (double)g.pos_pos.size() * 4 + (double)g.h2h_size * 4) / MB;
+    label_mb = ((double)(g.n + 1) * 8 * 2 + (double)(g.pos_hash.empty() ? 0 : g.pos_hash[g.n]) * 4 +
+                (double)g.h2h_size * 4) / MB;
   } else {                                             // beforeH2H_noHub, TreeStructure.cu:69-70
     label_mb = ((double)8 * 2 * g.n + (double)g.decomposition_size * 4 + (double)g.h2h_size * 4) / MB;
   }

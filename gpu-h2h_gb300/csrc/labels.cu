@@ -40,6 +40,9 @@ void DeviceIndex::release_labels() {
 
 void DeviceIndex::release() {
   release_labels();
+  lists = ListStore();
+  x_base = pos_base = 0;
+  id_base = 0;
   for (void *p : owned_rmq) cudaFree(p);
   owned_rmq.clear();
   first = rmq_id = nullptr;
@@ -359,19 +362,57 @@ __global__ void max_label_kernel(const int *dis, int64_t n, int *out) {
   if ((threadIdx.x & 31) == 0) atomicMax(out, m);
 }
 
-// Shortcut weights of every pos entry, read from the contraction's final
-// lists (slot_off / slot_w, forest vertex ids): entry k of v takes list
-// index pos_src[k] of v's list, or 0 for v itself.  One warp per vertex.
-__global__ void gather_pos_weights_kernel(const int64_t *pos_hash, const int *pos_src, const int64_t *slot_off,
-                                          const int *slot_w, int *pos_w, int n) {
+// Shortcut weights of every pos entry, read from the contraction's lists:
+// entry k of v takes list index pos_src[k] of v's list, or 0 for v itself.
+// One warp per vertex.
+__global__ void gather_pos_weights_kernel(const int64_t *pos_hash, const int *pos_src, const int64_t *list_off,
+                                          const int *list_w, int *pos_w, int n) {
   const int lane = threadIdx.x & 31;
   for (int64_t v = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; v < n;
        v += (gridDim.x * (int64_t)blockDim.x) >> 5) {
-    const int64_t b = pos_hash[v], e = pos_hash[v + 1], so = slot_off[v];
+    const int64_t b = pos_hash[v], e = pos_hash[v + 1], so = list_off[v];
     for (int64_t k = b + lane; k < e; k += 32) {
       const int src = pos_src[k];
-      pos_w[k] = src < 0 ? 0 : slot_w[so + src];
+      pos_w[k] = src < 0 ? 0 : list_w[so + src];
     }
+  }
+}
+
+// Position lists (mallocH2HLabel_noHub, H2HConsturction.cu:656-700): X(v)
+// and v itself ordered by position (depth - 1 of the member).  Positions of
+// one list are distinct, so an entry's slot is the number of smaller
+// positions in the list.  One block per vertex, the list's positions staged
+// in shared memory.  A member that is not a proper ancestor (position >=
+// d - 1) sets *err = 5.
+__global__ void build_positions_kernel(const int64_t *list_off, const int *list_id, const int *list_w,
+                                       const int *depth, const int64_t *pos_hash, int *pos_pos, int *pos_id,
+                                       int *pos_w, int *pos_src, int *err, int n) {
+  extern __shared__ int keys[];
+  const int tid = threadIdx.x, T = blockDim.x;
+  for (int v = blockIdx.x; v < n; v += gridDim.x) {
+    const int64_t b = list_off[v];
+    const int m = (int)(list_off[v + 1] - b);
+    const int d = depth[v];
+    const int64_t pb = pos_hash[v];
+    for (int i = tid; i <= m; i += T) {
+      int key = d - 1;
+      if (i < m) {
+        key = depth[list_id[b + i]] - 1;
+        if (key < 0 || key >= d - 1) atomicCAS(err, 0, 5);
+      }
+      keys[i] = key;
+    }
+    __syncthreads();
+    for (int i = tid; i <= m; i += T) {
+      const int key = keys[i];
+      int r = 0;
+      for (int j = 0; j <= m; j++) r += keys[j] < key;
+      pos_pos[pb + r] = key;
+      pos_id[pb + r] = i < m ? list_id[b + i] : v;
+      pos_w[pb + r] = i < m ? list_w[b + i] : 0;
+      pos_src[pb + r] = i < m ? i : -1;
+    }
+    __syncthreads();
   }
 }
 
@@ -413,7 +454,8 @@ bool TilePolicy::parse(const std::string &text) {
   return true;
 }
 
-FillPlan::FillPlan(const std::vector<Graph *> &graphs, const TilePolicy &pol) : gs(graphs), policy(pol) {
+FillPlan::FillPlan(const std::vector<Graph *> &graphs, const TilePolicy &pol, const ListStore &lst)
+    : gs(graphs), policy(pol), lists(lst) {
   const int K = (int)gs.size();
   GH_CHECK(K >= 1, H2H_ERR_ARG, "no graph to label");
   vbase.assign(K, 0);
@@ -432,8 +474,10 @@ FillPlan::FillPlan(const std::vector<Graph *> &graphs, const TilePolicy &pol) : 
   for (const Graph *g : gs) host_threads = std::max(host_threads, g->threads);
   host_threads = std::min(host_threads, K);
   std::vector<int64_t> f_drow(N + 1, 0), f_pos_hash(N + 1, 0);
-  std::vector<int> f_pos_pos(pos_total), f_pos_id(pos_total), f_pos_w(pos_total), f_pos_src(pos_total);
   std::vector<int> f_father(N), f_depth(N), f_hld(N);
+  int max_m = 0;
+  for (const Graph *g : gs)
+    for (int v = 0; v < g->n; v++) max_m = std::max<int64_t>(max_m, g->x_off[v + 1] - g->x_off[v]);
   std::vector<int64_t> sbase(K, 0);
   int64_t seg_total = 0;
   for (int i = 0; i < K; i++) {
@@ -462,13 +506,6 @@ FillPlan::FillPlan(const std::vector<Graph *> &graphs, const TilePolicy &pol) : 
           f_htop[V] = g.htop[v] + vb;
           f_hpos[V] = g.hpos[v] + vb;
           f_seg_off[V] = sbase[i] + g.seg_off[v];
-        }
-        const int64_t np = g.pos_hash[g.n];
-        for (int64_t k = 0; k < np; k++) {
-          f_pos_pos[pb + k] = g.pos_pos[k];
-          f_pos_id[pb + k] = g.pos_id[k] + vb;
-          f_pos_w[pb + k] = g.pos_w[k];
-          f_pos_src[pb + k] = g.pos_src.empty() ? -1 : g.pos_src[k];
         }
       }
     });
@@ -503,13 +540,21 @@ FillPlan::FillPlan(const std::vector<Graph *> &graphs, const TilePolicy &pol) : 
     err = dalloc<int>(1, work_bytes);
     GH_CUDA(cudaMemcpy(drow, f_drow.data(), sizeof(int64_t) * (N + 1), cudaMemcpyHostToDevice));
     GH_CUDA(cudaMemcpy(pos_hash, f_pos_hash.data(), sizeof(int64_t) * (N + 1), cudaMemcpyHostToDevice));
-    GH_CUDA(cudaMemcpy(pos_pos, f_pos_pos.data(), sizeof(int) * pos_total, cudaMemcpyHostToDevice));
-    GH_CUDA(cudaMemcpy(pos_id, f_pos_id.data(), sizeof(int) * pos_total, cudaMemcpyHostToDevice));
-    GH_CUDA(cudaMemcpy(pos_w, f_pos_w.data(), sizeof(int) * pos_total, cudaMemcpyHostToDevice));
-    GH_CUDA(cudaMemcpy(pos_src, f_pos_src.data(), sizeof(int) * pos_total, cudaMemcpyHostToDevice));
     GH_CUDA(cudaMemcpy(father, f_father.data(), sizeof(int) * N, cudaMemcpyHostToDevice));
     GH_CUDA(cudaMemcpy(depth, f_depth.data(), sizeof(int) * N, cudaMemcpyHostToDevice));
     GH_CUDA(cudaMemcpy(hld, f_hld.data(), sizeof(int) * N, cudaMemcpyHostToDevice));
+    {
+      const size_t ksmem = (size_t)(max_m + 1) * sizeof(int);
+      const int kdyn = enable_max_dynamic_smem(build_positions_kernel);
+      GH_CHECK(ksmem <= (size_t)kdyn, H2H_ERR_DEVICE, "separator too large for the position-list staging");
+      GH_CUDA(cudaMemset(err, 0, sizeof(int)));
+      build_positions_kernel<<<std::max(1, std::min(N, nsm * 16)), 128, ksmem>>>(
+          lists.off, lists.id, lists.w, depth, pos_hash, pos_pos, pos_id, pos_w, pos_src, err, N);
+      GH_CUDA(cudaGetLastError());
+      int e = 0;
+      GH_CUDA(cudaMemcpy(&e, err, sizeof(int), cudaMemcpyDeviceToHost));
+      GH_CHECK(e == 0, H2H_ERR_STATE, "an upper neighbour is not an ancestor in the tree");
+    }
     GH_CUDA(cudaMemcpy(seg_off, f_seg_off.data(), sizeof(int64_t) * (N + 1), cudaMemcpyHostToDevice));
     GH_CUDA(cudaMemcpy(htop, f_htop.data(), sizeof(int) * N, cudaMemcpyHostToDevice));
     GH_CUDA(cudaMemcpy(hpos, f_hpos.data(), sizeof(int) * N, cudaMemcpyHostToDevice));
@@ -645,12 +690,10 @@ void FillPlan::build_tiles(const TilePolicy &pol) {
   blocks = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)nsm * per_sm, ntiles));
 }
 
-void FillPlan::enqueue(cudaStream_t s, const int64_t *slot_off, const int *slot_w, cudaEvent_t *fill_ev) {
-  if (slot_off) {
-    gather_pos_weights_kernel<<<std::max(1, std::min(8192, (N * 32 + 255) / 256)), 256, 0, s>>>(
-        pos_hash, pos_src, slot_off, slot_w, pos_w, N);
-    GH_CUDA(cudaGetLastError());
-  }
+void FillPlan::enqueue(cudaStream_t s, cudaEvent_t *fill_ev) {
+  gather_pos_weights_kernel<<<std::max(1, std::min(8192, (N * 32 + 255) / 256)), 256, 0, s>>>(
+      pos_hash, pos_src, lists.off, lists.w, pos_w, N);
+  GH_CUDA(cudaGetLastError());
   // rows start at INT_MAX: split tiles combine with atomicMin; padding stays defined
   fill_int_kernel<<<1024, 256, 0, s>>>(dis, dis_total, INT_MAX);
   GH_CUDA(cudaGetLastError());
@@ -721,6 +764,7 @@ void FillPlan::attach(bool first) {
       D.pos_id = pos_id;
       D.dis = dis;
       D.pos = f_pos_hash[vb + g.n] - f_pos_hash[vb];
+      D.pos_base = f_pos_hash[vb];
       D.dis_padded = f_drow[vb + g.n] - f_drow[vb];
       D.err = dalloc_owned<int>(1, D);
       D.bytes += (int64_t)(g.n + 1) * 16 + (int64_t)g.n * 8 + D.pos * 8 + D.dis_padded * 4;
@@ -775,7 +819,7 @@ std::string tile_policy_tune(FillPlan &plan, ElimPlan &elim, cudaStream_t s, int
     }
     float best = 1e30f;
     for (int rep = 0; rep < 2; rep++) {
-      plan.enqueue(s, elim.slot_off, elim.slot_w, ev);
+      plan.enqueue(s, ev);
       plan.check_error();
       float ms = 0;
       GH_CUDA(cudaEventElapsedTime(&ms, ev[0], ev[1]));
@@ -831,7 +875,7 @@ void fill_labels_gpu(Graph &g) {
     TilePolicy pol;
     if (const char *e = std::getenv("GPUH2H_TILE_POLICY"))
       GH_CHECK(pol.parse(e), H2H_ERR_ARG, "GPUH2H_TILE_POLICY: expected 8 entries small_work/col_block/sep_chunk");
-    FillPlan plan({&g}, pol);
+    FillPlan plan({&g}, pol, D.lists);
     GH_CUDA(cudaDeviceSynchronize());
     g.t.translate_labels = clk.us();
     clk.reset();
@@ -840,7 +884,7 @@ void fill_labels_gpu(Graph &g) {
     GH_CUDA(cudaEventCreate(&ev[1]));
     float ms = 0;
     try {
-      plan.enqueue(0, nullptr, nullptr, ev);
+      plan.enqueue(0, ev);
       plan.check_error();
       GH_CUDA(cudaEventElapsedTime(&ms, ev[0], ev[1]));
     } catch (...) {
@@ -856,6 +900,7 @@ void fill_labels_gpu(Graph &g) {
   }
   D.release_labels();
   D.n = n;
+  D.pos_base = 0;
   // padded row offsets
   std::vector<int64_t> drow(n + 1, 0);
   for (int v = 0; v < n; v++) drow[v + 1] = drow[v] + ((g.depth[v] + 3) & ~3);
@@ -958,6 +1003,25 @@ void fill_labels_gpu(Graph &g) {
 }
 
 // Copies the filled labels back into the reference's unpadded layout.
+// Position lists in the reference layout with graph-local ids: the host
+// copies (L3) or the graph's range of the device arrays (L4).
+void download_positions(const Graph &g, int *pos_id, int *pos_pos) {
+  const int64_t np = g.pos_hash.empty() ? 0 : g.pos_hash[g.n];
+  if ((int64_t)g.pos_id.size() == np && np) {
+    if (pos_id) std::copy(g.pos_id.begin(), g.pos_id.end(), pos_id);
+    if (pos_pos) std::copy(g.pos_pos.begin(), g.pos_pos.end(), pos_pos);
+    return;
+  }
+  GH_CHECK(g.dev.pos_id && g.dev.pos_pos && g.dev.pos == np, H2H_ERR_STATE, "position lists not on the device");
+  if (!np) return;
+  if (pos_pos) GH_CUDA(cudaMemcpy(pos_pos, g.dev.pos_pos + g.dev.pos_base, sizeof(int) * np, cudaMemcpyDeviceToHost));
+  if (pos_id) {
+    GH_CUDA(cudaMemcpy(pos_id, g.dev.pos_id + g.dev.pos_base, sizeof(int) * np, cudaMemcpyDeviceToHost));
+    if (g.dev.id_base)
+      for (int64_t k = 0; k < np; k++) pos_id[k] -= g.dev.id_base;
+  }
+}
+
 // The graph's rows are [drow_host[0], drow_host[n]) of the device array
 // (a batch's forest array holds other graphs' rows around them).
 void download_labels(const Graph &g, int *dis_out) {

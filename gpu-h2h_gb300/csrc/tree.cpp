@@ -1,14 +1,13 @@
 // tree.cpp -- tree decomposition structure and label layout on the host:
-//   getrank / getTreeStructure / makeOULAAndRMQ / OULADFS (TreeStructure.cu:102-262)
-//   mallocH2HLabel_noHub (H2HConsturction.cu:618-722)
+//   getTreeStructure / OULADFS (TreeStructure.cu:102-262): children, Euler
+//     tour, depths, from the fathers the contraction picked on the GPU
+//   mallocH2HLabel_noHub (H2HConsturction.cu:618-722): row and position
+//     offsets (the position lists themselves are built on the GPU for L4)
 //   constructBFSTree     (H2HConsturction.cu:324-377)
 //
 // The Euler tour is walked with an explicit stack (the reference recurses),
 // children in increasing id order as Childs lists them.  The sparse table is
-// built directly in the reference's compacted form: row i keeps levels
-// 0..floor(log2(L - i)) (exactly the entries the reference's dense table
-// fills with a valid depth before it compacts at the first unfilled one), and
-// ties keep the left entry (`<=`, TreeStructure.cu:218).
+// built on the GPU (query.cu).
 #include <algorithm>
 #include <atomic>
 
@@ -20,18 +19,10 @@ namespace gh {
 void build_tree(Graph &g) {
   Clock clk;
   const int n = g.n;
-  std::vector<int> rank(n, -1);
-  for (int i = 0; i < n; i++) rank[g.elim[i]] = i;
+  GH_CHECK((int)g.father.size() == n, H2H_ERR_STATE, "fathers missing");
   g.head = g.elim[n - 1];
-  g.father.assign(n, -1);
-  for (int v = 0; v < n; v++) {
-    int best = INT32_MAX, f = -1;
-    for (int64_t k = g.x_off[v]; k < g.x_off[v + 1]; k++) {
-      int a = g.x_id[k];
-      if (rank[a] < best) { best = rank[a]; f = a; }
-    }
-    g.father[v] = f;
-  }
+  for (int v = 0; v < n; v++)
+    GH_CHECK((g.father[v] < 0) == (v == g.head), H2H_ERR_STATE, "decomposition is not a single tree");
   std::vector<int> cnt(n, 0);
   for (int v = 0; v < n; v++) if (g.father[v] >= 0) cnt[g.father[v]]++;
   g.child_off.assign(n + 1, 0);
@@ -91,40 +82,42 @@ void allocate_labels_and_bfs(Graph &g) {
     g.dis_hash[v + 1] = g.dis_hash[v] + g.depth[v];
     g.pos_hash[v + 1] = g.pos_hash[v] + (g.x_off[v + 1] - g.x_off[v]) + 1;
   }
-  g.pos_id.resize(g.pos_hash[n]);
-  g.pos_pos.resize(g.pos_hash[n]);
-  g.pos_w.resize(g.pos_hash[n]);
-  g.pos_src.resize(g.pos_hash[n]);
-  Pool pool(g.threads);
-  std::atomic<int> bad{-1};
-  pool.parallel_for(n, 1024, [&](int64_t b, int64_t e, int) {
-    struct Entry {
-      int64_t key;  // position << 32 | id
-      int w, src;
-      bool operator<(const Entry &o) const { return key < o.key; }
-    };
-    std::vector<Entry> tmp;
-    for (int64_t vv = b; vv < e; vv++) {
-      const int v = (int)vv;
-      const int d = g.depth[v];
-      tmp.clear();
-      for (int64_t k = g.x_off[v]; k < g.x_off[v + 1]; k++) {
-        int a = g.x_id[k], p = g.depth[a] - 1;
-        if (p < 0 || p >= d - 1) { bad = v; continue; }
-        tmp.push_back({(int64_t)p << 32 | (uint32_t)a, g.x_w[k], (int)(k - g.x_off[v])});
+  // host position lists only for L3 (its level fill runs from them); L4
+  // builds them on the GPU from the device lists
+  if (g.label_mode == H2H_LABEL_L3) {
+    if ((int64_t)g.x_id.size() != g.x_off[n]) download_lists(g);
+    g.pos_id.resize(g.pos_hash[n]);
+    g.pos_pos.resize(g.pos_hash[n]);
+    g.pos_w.resize(g.pos_hash[n]);
+    Pool pool(g.threads);
+    std::atomic<int> bad{-1};
+    pool.parallel_for(n, 1024, [&](int64_t b, int64_t e, int) {
+      std::vector<std::pair<int64_t, int>> tmp;
+      for (int64_t vv = b; vv < e; vv++) {
+        const int v = (int)vv;
+        const int d = g.depth[v];
+        tmp.clear();
+        for (int64_t k = g.x_off[v]; k < g.x_off[v + 1]; k++) {
+          int a = g.x_id[k], p = g.depth[a] - 1;
+          if (p < 0 || p >= d - 1) { bad = v; continue; }
+          tmp.push_back({(int64_t)p << 32 | (uint32_t)a, g.x_w[k]});
+        }
+        tmp.push_back({(int64_t)(d - 1) << 32 | (uint32_t)v, 0});
+        std::sort(tmp.begin(), tmp.end());  // positions are distinct
+        int64_t o = g.pos_hash[v];
+        for (size_t k = 0; k < tmp.size(); k++) {
+          g.pos_pos[o + k] = (int)(tmp[k].first >> 32);
+          g.pos_id[o + k] = (int)(tmp[k].first & 0xffffffff);
+          g.pos_w[o + k] = tmp[k].second;
+        }
       }
-      tmp.push_back({(int64_t)(d - 1) << 32 | (uint32_t)v, 0, -1});
-      std::sort(tmp.begin(), tmp.end());  // positions are distinct
-      int64_t o = g.pos_hash[v];
-      for (size_t k = 0; k < tmp.size(); k++) {
-        g.pos_pos[o + k] = (int)(tmp[k].key >> 32);
-        g.pos_id[o + k] = (int)(tmp[k].key & 0xffffffff);
-        g.pos_w[o + k] = tmp[k].w;
-        g.pos_src[o + k] = tmp[k].src;
-      }
-    }
-  });
-  GH_CHECK(bad.load() < 0, H2H_ERR_STATE, "an upper neighbour is not an ancestor in the tree");
+    });
+    GH_CHECK(bad.load() < 0, H2H_ERR_STATE, "an upper neighbour is not an ancestor in the tree");
+  } else {
+    std::vector<int>().swap(g.pos_id);
+    std::vector<int>().swap(g.pos_pos);
+    std::vector<int>().swap(g.pos_w);
+  }
   g.t.malloc_labels = clk.us();
   clk.reset();
   // level order from the head, children in Childs order

@@ -188,8 +188,8 @@ int h2h_batch_set_weights(h2h_batch *b, int index, const int *w);
  * shape depends only on the arcs, not on their weights, so it is kept).
  * Waits for the result; the graphs' queries see the new labels. */
 int h2h_batch_rebuild(h2h_batch *b);
-/* Brings the host copies of the shortcut weights (h2h_copy_adj) in line
- * with the last rebuild. */
+/* Waits for the batch's stream.  Accessors (h2h_copy_adj, h2h_copy_labels)
+ * read the device arrays, so they see the last rebuild once it returned. */
 int h2h_batch_sync_host(h2h_batch *b);
 /* Tile shapes of the forest label fill.  policy is 8 entries
  * "small_work/col_block/sep_chunk" separated by spaces: level width below /
