@@ -125,18 +125,27 @@ __device__ void merge_neighbour(const ElimArgs &A, int u, int wu, int iu, int v,
   const int s = __ldcg(A.lsize + u);
   const int J = __ldcg(A.ljunk + u);
   int np = 0;
-  for (int base = J; base < s; base += 32) {
-    const int idx = base + lane;
-    int x = INT_MAX, w = 0;
-    if (idx < s) { x = __ldcg(A.slot_nbr + off + idx); w = __ldcg(A.slot_w + off + idx); }
-    const bool keep = idx < s && x != v;
-    const unsigned bal = __ballot_sync(0xffffffffu, keep);
-    if (keep) {
-      const int pos = np + __popc(bal & ((1u << lane) - 1u));
-      pid[pos] = x;
-      pw[pos] = w;
+  // u's list minus v, loaded four warp-widths at a time so the L2 round trips overlap
+  for (int base = J; base < s; base += 128) {
+    int x[4], w[4];
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+      const int idx = base + r * 32 + lane;
+      x[r] = INT_MAX;
+      w[r] = 0;
+      if (idx < s) { x[r] = __ldcg(A.slot_nbr + off + idx); w[r] = __ldcg(A.slot_w + off + idx); }
     }
-    np += __popc(bal);
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+      const bool keep = base + r * 32 + lane < s && x[r] != v;
+      const unsigned bal = __ballot_sync(0xffffffffu, keep);
+      if (keep) {
+        const int pos = np + __popc(bal & ((1u << lane) - 1u));
+        pid[pos] = x[r];
+        pw[pos] = w[r];
+      }
+      np += __popc(bal);
+    }
   }
   __syncwarp();
   const int nq = c - 1;
@@ -399,6 +408,196 @@ __global__ void __launch_bounds__(512) elim_kernel(ElimArgs A) {
       }
       __syncthreads();
     }
+  }
+}
+
+// The global order over levels <= C for one graph, spread over the whole
+// GPU.  The cluster kernel above gives one cell at most 16 SMs; the global
+// order of a large graph is one long chain of eliminations whose neighbour
+// merges want all of them.  One cooperative launch, one block per SM, one
+// grid barrier per elimination.  Candidate keys live in global arrays at a
+// fixed index per candidate; block b owns the index slice [lo_b, hi_b): it
+// alone merges the lists of the candidates in its slice, refreshes their
+// keys and marks its picked candidate dead, so once its merges are done it
+// can take the argmin of its slice.  Per elimination:
+//   every block reduces the per-block argmins to the same pick v (the key
+//   order is strict); block 0 records it and writes back the previous pick's
+//   compacted list (nobody reads that list any more); every block loads and
+//   compacts v's list into its shared memory (the same code as the cluster
+//   leader), merges those neighbours of v that fall in its slice, and writes
+//   the argmin of its slice                                  -- grid sync
+// Same key order, list rules and results as the cluster kernel in heap mode.
+struct HeapArgs {
+  ElimArgs E;          // heap_mode = 1; pstage (or shared memory) holds the per-warp merge buffers
+  int start, k;        // the cell: elim[start .. start + k)
+  int *cdeg, *ch, *cid;
+  unsigned char *dead;
+  int4 *partial;       // (deg + height, deg, id, index) per block
+};
+
+__device__ __forceinline__ void better(int &bs, int &bd, int &bi, int &bp, int s, int d, int i, int p) {
+  if (p >= 0 && (bp < 0 || key_less(s, d, i, bs, bd, bi))) { bs = s; bd = d; bi = i; bp = p; }
+}
+
+// Block-wide argmin of (s, d, i, p) tuples; the result is valid in thread 0.
+__device__ __forceinline__ void block_best(int &bs, int &bd, int &bi, int &bp, int *rs, int *rd, int *ri, int *rp) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int o = 16; o > 0; o >>= 1) {
+    const int os = __shfl_down_sync(0xffffffffu, bs, o), od = __shfl_down_sync(0xffffffffu, bd, o);
+    const int oi = __shfl_down_sync(0xffffffffu, bi, o), op = __shfl_down_sync(0xffffffffu, bp, o);
+    better(bs, bd, bi, bp, os, od, oi, op);
+  }
+  if (lane == 0) { rs[wid] = bs; rd[wid] = bd; ri[wid] = bi; rp[wid] = bp; }
+  __syncthreads();
+  if (threadIdx.x == 0)
+    for (int w = 1; w < nw; w++) better(bs, bd, bi, bp, rs[w], rd[w], ri[w], rp[w]);
+}
+
+__global__ void __launch_bounds__(512, 1) heap_grid_kernel(HeapArgs H) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ int s_rs[32], s_rd[32], s_ri[32], s_rp[32];
+  __shared__ int s_bc[4];  // v, height of the pick, |own list|, index of the pick
+  __shared__ int s_nmine;
+  cg::grid_group grid = cg::this_grid();
+  const ElimArgs &A = H.E;
+  const int tid = threadIdx.x, nthr = blockDim.x, lane = tid & 31, wid = tid >> 5, nw = nthr >> 5;
+  const int b = blockIdx.x, G = gridDim.x;
+  const int lal = (A.lmax + 3) & ~3;
+  int *aid = (int *)smem;
+  int *aw = aid + lal;
+  int *mine = aw + lal;    // indices into aid of the neighbours this block merges
+  int *pid, *pw;           // this warp's merge buffers: shared memory when they fit, else global
+  if (A.pstage) {
+    pid = A.pstage + ((int64_t)b * nw + wid) * 2 * (int64_t)A.lmax;
+    pw = pid + A.lmax;
+  } else {
+    pid = mine + lal + (int64_t)wid * 2 * lal;
+    pw = pid + lal;
+  }
+  Cand cand;
+  cand.id = H.cid;
+  cand.deg = H.cdeg;
+  cand.third = H.ch;
+  const int lo = (int)((int64_t)H.k * b / G), hi = (int)((int64_t)H.k * (b + 1) / G);
+  // keys of this block's slice, then its first argmin
+  for (int i = lo + tid; i < hi; i += nthr) {
+    const int v = A.elim[H.start + i];
+    H.cid[i] = v;
+    H.cdeg[i] = A.key_deg0[v];
+    H.ch[i] = A.key_h0[v];
+    H.dead[i] = 0;
+    A.cpos[v] = i;
+  }
+  __syncthreads();
+  {
+    int bs = INT_MAX, bd = INT_MAX, bi = INT_MAX, bp = -1;
+    for (int i = lo + tid; i < hi; i += nthr) {
+      const int d = H.cdeg[i];
+      better(bs, bd, bi, bp, d + H.ch[i], d, H.cid[i], i);
+    }
+    block_best(bs, bd, bi, bp, s_rs, s_rd, s_ri, s_rp);
+    if (tid == 0) H.partial[b] = make_int4(bs, bd, bi, bp);
+  }
+  int prev_v = -1, prev_c = 0;
+  grid.sync();
+  for (int j = 0; j < H.k; j++) {
+    // ---- the pick
+    {
+      int bs = INT_MAX, bd = INT_MAX, bi = INT_MAX, bp = -1;
+      for (int g = tid; g < G; g += nthr) {
+        const int4 q = __ldcg(H.partial + g);
+        better(bs, bd, bi, bp, q.x, q.y, q.z, q.w);
+      }
+      block_best(bs, bd, bi, bp, s_rs, s_rd, s_ri, s_rp);
+      if (tid == 0) {  // bp >= 0: j < k candidates remain
+        s_bc[0] = bi;
+        s_bc[1] = __ldcg(H.ch + bp);
+        s_bc[3] = bp;
+        s_nmine = 0;
+        if (b == 0) A.elim[H.start + j] = bi;
+        if (bp >= lo && bp < hi) {  // the owner retires the candidate
+          H.dead[bp] = 1;
+          A.cpos[bi] = -1;
+        }
+      }
+    }
+    // block 0: the previous pick's list, read by nobody since the barrier
+    if (b == 0 && prev_v >= 0) {
+      const int64_t off = __ldcg(A.slot_off + prev_v);
+      for (int i = tid; i < prev_c; i += nthr) { A.slot_nbr[off + i] = aid[i]; A.slot_w[off + i] = aw[i]; }
+      if (tid == 0) { A.lsize[prev_v] = prev_c; A.ljunk[prev_v] = 0; }
+    }
+    __syncthreads();
+    const int v = s_bc[0], hnow = s_bc[1];
+    const int64_t voff = __ldcg(A.slot_off + v);
+    const int vJ = __ldcg(A.ljunk + v);
+    const int sv = __ldcg(A.lsize + v) - vJ;
+    if (sv > A.lmax) {  // every block sees the same sizes: all leave together
+      if (b == 0 && tid == 0) set_err(A.err, kErrStaging);
+      return;
+    }
+    // ---- v's own list (every block the same copy)
+    for (int i = tid; i < sv; i += nthr) {
+      aid[i] = __ldcg(A.slot_nbr + voff + vJ + i);
+      aw[i] = __ldcg(A.slot_w + voff + vJ + i);
+    }
+    __syncthreads();
+    bool dup = false;
+    for (int i = tid + 1; i < sv; i += nthr)
+      if (aid[i] == aid[i - 1]) dup = true;
+    dup = __syncthreads_or(dup);
+    if (tid == 0) {
+      int c = sv;
+      if (dup) {  // carry merge (the later entry keeps the smaller weight), then compaction
+        for (int i = 1; i < sv; i++) {
+          if (aid[i] == aid[i - 1] && aid[i] != INT_MAX) {
+            if (aw[i - 1] < aw[i]) aw[i] = aw[i - 1];
+            aid[i - 1] = INT_MAX;
+          }
+        }
+        c = 0;
+        for (int i = 0; i < sv; i++) if (aid[i] != INT_MAX) { aid[c] = aid[i]; aw[c] = aw[i]; c++; }
+      }
+      s_bc[2] = c;
+    }
+    __syncthreads();
+    const int c = s_bc[2];
+    // ---- the neighbours in this block's slice
+    for (int i = tid; i < c; i += nthr) {
+      const int p = __ldcg(A.cpos + aid[i]);
+      if ((p >= lo && p < hi) || (p < 0 && b == 0)) mine[atomicAdd(&s_nmine, 1)] = i;
+    }
+    __syncthreads();
+    const int nm = s_nmine;
+    for (int t = wid; t < nm; t += nw) {
+      const int i = mine[t];
+      const int u = aid[i];
+      if (__ldcg(A.lsize + u) - __ldcg(A.ljunk + u) > A.lmax) {
+        if (lane == 0) set_err(A.err, kErrStaging);
+        continue;
+      }
+      merge_neighbour(A, u, aw[i], i, v, hnow, aid, aw, c, pid, pw, lane, cand);
+    }
+    __syncthreads();
+    // ---- the argmin of this block's slice, keys final (only this block writes them)
+    {
+      int bs = INT_MAX, bd = INT_MAX, bi = INT_MAX, bp = -1;
+      for (int i = lo + tid; i < hi; i += nthr)
+        if (!H.dead[i]) {
+          const int d = __ldcg(H.cdeg + i);
+          better(bs, bd, bi, bp, d + __ldcg(H.ch + i), d, H.cid[i], i);
+        }
+      block_best(bs, bd, bi, bp, s_rs, s_rd, s_ri, s_rp);
+      if (tid == 0) H.partial[b] = make_int4(bs, bd, bi, bp);
+    }
+    prev_v = v;
+    prev_c = c;
+    grid.sync();
+  }
+  if (b == 0 && prev_v >= 0) {
+    const int64_t off = __ldcg(A.slot_off + prev_v);
+    for (int i = tid; i < prev_c; i += nthr) { A.slot_nbr[off + i] = aid[i]; A.slot_w[off + i] = aw[i]; }
+    if (tid == 0) { A.lsize[prev_v] = prev_c; A.ljunk[prev_v] = 0; }
   }
 }
 
@@ -678,6 +877,7 @@ ElimPlan::ElimPlan(const std::vector<Graph *> &graphs) : gs(graphs) {
   // launch with its own cluster size (a large cell spreads its merges over up
   // to 16 CTAs), and the groups of a step run side by side on forked streams.
   const int smem_dyn = enable_max_dynamic_smem(elim_kernel);
+  const int smem_dyn_hg = enable_max_dynamic_smem(heap_grid_kernel);
   GH_CUDA(cudaFuncSetAttribute(elim_kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
   int dev = 0;
   GH_CUDA(cudaGetDevice(&dev));
@@ -793,13 +993,41 @@ ElimPlan::ElimPlan(const std::vector<Graph *> &graphs) : gs(graphs) {
         cudaGetLastError();
       }
       Lc.cs = cs;
+      Lc.grid_heap = false;
+      if (heap && Lc.ncell == 1 && K == 1 && !std::getenv("GPUH2H_CLUSTER_HEAP")) {
+        // one graph's global order: all SMs in one cooperative launch when
+        // the eliminated list fits shared memory; per-warp merge buffers in
+        // shared memory too when 4+ warps' worth fit (a merge walks them
+        // serially), else 16 warps with buffers in global memory
+        const int64_t own = 3 * al(4LL * Lc.lmax), per_warp = 2 * al(4LL * Lc.lmax);
+        const int64_t fit = own <= smem_dyn_hg ? (smem_dyn_hg - own) / per_warp : 0;
+        const int hw = fit >= 4 ? (int)std::min<int64_t>(16, fit) : 16;
+        const int64_t hsmem = fit >= 4 ? own + hw * per_warp : own;
+        int per = 0;
+        if (own <= smem_dyn_hg &&
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, heap_grid_kernel, hw * 32, (size_t)hsmem) ==
+                cudaSuccess &&
+            per >= 1) {
+          Lc.grid_heap = true;
+          Lc.cs = 1;
+          Lc.nw = hw;
+          Lc.smem = hsmem;
+          Lc.global_stage = fit < 4;
+        }
+        cudaGetLastError();
+      }
       Lc.pstage_off = step_pstage;
-      if (Lc.global_stage) step_pstage += (int64_t)Lc.ncell * cs * nw * 2 * (int64_t)Lc.lmax;
+      if (Lc.grid_heap) {
+        if (Lc.global_stage) step_pstage += (int64_t)nsm * Lc.nw * 2 * (int64_t)Lc.lmax;
+      }
+      else if (Lc.global_stage) step_pstage += (int64_t)Lc.ncell * cs * nw * 2 * (int64_t)Lc.lmax;
       launches.push_back(Lc);
       g0 = g1;
     }
     pstage_ints = std::max(pstage_ints, step_pstage);
   }
+  heap_cell_start = fcs.empty() ? 0 : fcs.back();
+  heap_cell_count = fcc.empty() ? 0 : fcc.back();
   {
     // side streams for the groups of a step beyond the first
     int most = 1;
@@ -837,6 +1065,14 @@ ElimPlan::ElimPlan(const std::vector<Graph *> &graphs) : gs(graphs) {
     adj_w = palloc<int>(std::max<int64_t>(M, 1), bytes);
     heap_verts = palloc<int>(std::max(heap_total, 1), bytes);
     if (pstage_ints) pstage = palloc<int>(pstage_ints, bytes);
+    for (const Launch &Lc : launches)
+      if (Lc.grid_heap) {
+        hg_deg = palloc<int>(Lc.kmax, bytes);
+        hg_h = palloc<int>(Lc.kmax, bytes);
+        hg_id = palloc<int>(Lc.kmax, bytes);
+        hg_dead = palloc<unsigned char>(Lc.kmax, bytes);
+        hg_partial = palloc<int4>(nsm, bytes);
+      }
     for (int k = 1; k < max_group; k++) {
       cudaStream_t st = nullptr;
       cudaEvent_t e = nullptr;
@@ -872,6 +1108,10 @@ void ElimPlan::release() {
                 elim_init, deg0, deg_init, h0, cpos, err, ljunk, cell_start, cell_count, adj_off, adj_v, adj_w,
                 heap_verts, pstage};
   for (void *p : ps) cudaFree(p);
+  cudaFree(hg_deg); cudaFree(hg_h); cudaFree(hg_id); cudaFree(hg_dead); cudaFree(hg_partial);
+  hg_deg = hg_h = hg_id = nullptr;
+  hg_dead = nullptr;
+  hg_partial = nullptr;
   cudaFree(rank);
   cudaFree(father_dev);
   rank = father_dev = nullptr;
@@ -916,16 +1156,44 @@ void ElimPlan::launch_one(const Launch &Lc, cudaStream_t s, bool trace) {
   cfg.stream = s;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   if (trace) { cudaEventCreate(&ev0); cudaEventCreate(&ev1); cudaEventRecord(ev0, s); }
-  GH_CUDA(cudaLaunchKernelEx(&cfg, elim_kernel, A));
+  if (Lc.grid_heap) {
+    HeapArgs H;
+    H.E = A;
+    H.start = 0;
+    H.k = 0;
+    {
+      // the heap cell's start and size (host copies of the cell table entry)
+      H.start = heap_cell_start;
+      H.k = heap_cell_count;
+    }
+    H.cdeg = hg_deg;
+    H.ch = hg_h;
+    H.cid = hg_id;
+    H.dead = hg_dead;
+    H.partial = (int4 *)hg_partial;
+    cudaLaunchAttribute ca[1];
+    ca[0].id = cudaLaunchAttributeCooperative;
+    ca[0].val.cooperative = 1;
+    cudaLaunchConfig_t cc = {};
+    cc.attrs = ca;
+    cc.numAttrs = 1;
+    cc.blockDim = dim3(Lc.nw * 32);
+    cc.gridDim = dim3(nsm);
+    cc.dynamicSmemBytes = (size_t)Lc.smem;
+    cc.stream = s;
+    if (H.k > 0) GH_CUDA(cudaLaunchKernelEx(&cc, heap_grid_kernel, H));
+  } else {
+    GH_CUDA(cudaLaunchKernelEx(&cfg, elim_kernel, A));
+  }
   if (trace) {
     cudaEventRecord(ev1, s);
     cudaEventSynchronize(ev1);
     float ms = 0;
     cudaEventElapsedTime(&ms, ev0, ev1);
     std::fprintf(stderr,
-                 "[gpuh2h] elim %s %d: %d cells x %d CTAs x %d warps, kmax %d, lmax %d, smem %lld, slots %d%s: %.3f ms\n",
+                 "[gpuh2h] elim %s %d: %d cells x %d CTAs x %d warps, kmax %d, lmax %d, smem %lld, slots %d%s%s: %.3f ms\n",
                  Lc.heap ? "heap" : "level", Lc.level, Lc.ncell, Lc.cs, Lc.nw, Lc.kmax, Lc.lmax, (long long)Lc.smem,
-                 Lc.slots, Lc.global_stage ? " (global merge staging)" : "", ms);
+                 Lc.slots, Lc.global_stage ? " (global merge staging)" : "", Lc.grid_heap ? " (all SMs)" : "", ms);
     cudaEventDestroy(ev0);
     cudaEventDestroy(ev1);
   }

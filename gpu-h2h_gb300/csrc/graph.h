@@ -131,6 +131,7 @@ struct ElimPlan {
     int step, level, ncell, kmax, lmax, cs, nw, slots;
     int64_t lo, smem, pstage_off;
     bool heap, global_stage;
+    bool grid_heap;  // the global order of one graph as one cooperative launch over all SMs
   };
   std::vector<Graph *> gs;
   std::vector<int> vbase;
@@ -152,6 +153,11 @@ struct ElimPlan {
   unsigned long long *pool_next = nullptr, *pool_first = nullptr;
   ListStore lists;       // compact final lists (forest numbering), after build_lists()
   int *rank = nullptr, *father_dev = nullptr;
+  // candidate keys of the whole-GPU global order (heap_grid_kernel)
+  int *hg_deg = nullptr, *hg_h = nullptr, *hg_id = nullptr;
+  unsigned char *hg_dead = nullptr;
+  void *hg_partial = nullptr;
+  int heap_cell_start = 0, heap_cell_count = 0;  // the last cell of the table (one graph: its global order)
   int64_t bytes = 0;
   explicit ElimPlan(const std::vector<Graph *> &graphs);
   ~ElimPlan();
