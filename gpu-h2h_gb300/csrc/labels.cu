@@ -201,11 +201,12 @@ long long spin_limit_cycles() {
 }
 
 struct FlowArgs {
-  // tiles in BFS node order: tile t covers columns [c0, c1) of node tile_node[t]
-  // and separator members [u0, u1) of X(v)\{v}
-  const int *tile_node, *tile_c0, *tile_c1, *tile_u0, *tile_u1;
+  // tiles in forest BFS order: ticket t belongs to node tile_node[t]; the
+  // node's tiles are tickets node_first .. + node_ntiles, its column blocks
+  // (node_cb columns) outer and separator chunks (node_sc members) inner
+  const int *tile_node;
   int ntiles;
-  const int *node_ntiles;  // tiles per node
+  const int *node_first, *node_ntiles, *node_cb, *node_sc;
   int *node_cnt;           // finished tiles per node
   const int *father;
   const int *depth;
@@ -240,62 +241,72 @@ __device__ __forceinline__ int ld_relaxed(const int *p) {
   return v;
 }
 
+// Every warp is an independent worker: it takes a ticket, stages the tile's
+// separator entries and the node's root-path segments in its own slice of
+// shared memory while lane 0 waits for the father, sweeps the columns (lane
+// per column) and publishes; only warp-level barriers, so a thin tile or a
+// dependency wait stalls one warp, not a CTA.
 __global__ void __launch_bounds__(128) fill_flow_kernel(FlowArgs A) {
   extern __shared__ __align__(16) unsigned char smem[];
-  __shared__ int s_t, s_stop;
-  const int tid = threadIdx.x, T = blockDim.x;
-  int64_t *xs_row = (int64_t *)smem;                 // [max_u]
-  int *xs_p = (int *)(xs_row + A.max_u);             // [max_u]
-  int *xs_w = xs_p + A.max_u;                        // [max_u]
-  int *s_top = xs_w + A.max_u;                       // [max_segs]
-  int *s_pos = s_top + A.max_segs;                   // [max_segs]
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int ual = (A.max_u + 1) & ~1, sal = (A.max_segs + 1) & ~1;
+  unsigned char *mine = smem + (size_t)wid * ((size_t)ual * 16 + (size_t)sal * 8);
+  int64_t *xs_row = (int64_t *)mine;                 // [max_u]
+  int *xs_p = (int *)(xs_row + ual);                 // [max_u]
+  int *xs_w = xs_p + ual;                            // [max_u]
+  int *s_top = xs_w + ual;                           // [max_segs]
+  int *s_pos = s_top + sal;                          // [max_segs]
   for (;;) {
-    if (tid == 0) s_t = atomicAdd(A.next, 1);
-    __syncthreads();
-    const int t = s_t;
+    int t = 0;
+    if (lane == 0) t = atomicAdd(A.next, 1);
+    t = __shfl_sync(0xffffffffu, t, 0);
     if (t >= A.ntiles) return;
     const int v = __ldg(A.tile_node + t);
-    const int c0 = __ldg(A.tile_c0 + t), c1 = __ldg(A.tile_c1 + t);
-    const int u0 = __ldg(A.tile_u0 + t), u1 = __ldg(A.tile_u1 + t);
     const int d = __ldg(A.depth + v);
     const int f = __ldg(A.father + v);
-    if (tid == 0) {
-      s_stop = 0;
-      if (f >= 0) {
-        long long t0 = clock64();
-        while (ld_acquire(A.done + f) == 0) {
-          if (ld_relaxed(A.err) != 0 || clock64() - t0 > A.spin_limit) {
-            atomicCAS(A.err, 0, 4);
-            s_stop = 1;
-            break;
-          }
-          __nanosleep(64);
-        }
-      }
-    }
     const int64_t base = __ldg(A.drow + v);
     const int64_t pb = __ldg(A.pos_hash + v);
     const int m = (int)(__ldg(A.pos_hash + v + 1) - pb) - 1;   // X(v)\{v}
+    const int sub = t - __ldg(A.node_first + v);
+    const int cb = __ldg(A.node_cb + v), sc = __ldg(A.node_sc + v);
+    const int nuc = (max(m, 1) + sc - 1) / sc;
+    const int ci = sub / nuc, ui = sub - ci * nuc;
+    const int c0 = ci * cb, c1 = min(d, c0 + cb);
+    const int u0 = ui * sc, u1 = min(m, u0 + sc);
     const bool whole_sep = u0 == 0 && u1 == m;                  // this tile sees every member
     const int nu = u1 - u0;
-    // separator entries and the root-path segments need no finished row:
-    // stage them while thread 0 waits
-    for (int i = tid; i < nu; i += T) {
+    // separator entries and root-path segments need no finished row
+    for (int i = lane; i < nu; i += 32) {
       xs_p[i] = __ldg(A.pos_pos + pb + u0 + i);
       xs_w[i] = __ldg(A.pos_w + pb + u0 + i);
       xs_row[i] = __ldg(A.drow + __ldg(A.pos_id + pb + u0 + i));
     }
     const int64_t sb = __ldg(A.seg_off + v);
     const int ns = (int)(__ldg(A.seg_off + v + 1) - sb);
-    for (int i = tid; i < ns; i += T) {
+    for (int i = lane; i < ns; i += 32) {
       s_top[i] = __ldg(A.seg_top + sb + i);
       s_pos[i] = __ldg(A.seg_pos + sb + i);
     }
-    if (tid == 0 && c1 == d && u0 == 0) A.dis[base + d - 1] = 0;
-    __syncthreads();
-    if (s_stop) return;
+    int stop = 0;
+    if (lane == 0) {
+      if (f >= 0) {
+        long long t0 = clock64();
+        while (ld_acquire(A.done + f) == 0) {
+          if (ld_relaxed(A.err) != 0 || clock64() - t0 > A.spin_limit) {
+            atomicCAS(A.err, 0, 4);
+            stop = 1;
+            break;
+          }
+          __nanosleep(64);
+        }
+      }
+      if (c1 == d && u0 == 0) A.dis[base + d - 1] = 0;
+    }
+    stop = __shfl_sync(0xffffffffu, stop, 0);
+    __syncwarp();
+    if (stop) return;
     const int cend = min(c1, d - 1);
-    for (int j = c0 + tid; j < cend; j += T) {
+    for (int j = c0 + lane; j < cend; j += 32) {
       // ancestor at depth j + 1: last segment whose top depth is <= j + 1
       int lo = 0, hi = ns - 1;
       while (lo < hi) {
@@ -317,8 +328,8 @@ __global__ void __launch_bounds__(128) fill_flow_kernel(FlowArgs A) {
       if (whole_sep) A.dis[base + j] = r;
       else atomicMin(A.dis + base + j, r);
     }
-    __syncthreads();
-    if (tid == 0) {
+    __syncwarp();
+    if (lane == 0) {
       __threadfence();
       const int nt = __ldg(A.node_ntiles + v);
       if (nt == 1 || atomicAdd(A.node_cnt + v, 1) == nt - 1) {
@@ -326,6 +337,17 @@ __global__ void __launch_bounds__(128) fill_flow_kernel(FlowArgs A) {
         st_release(A.done + v, 1);
       }
     }
+    __syncwarp();  // the slice is restaged only after every lane left the sweep
+  }
+}
+
+// tile_node[t] = v for the tickets of every node v.  One warp per node.
+__global__ void expand_tiles_kernel(const int *node_first, const int *node_ntiles, int *tile_node, int n) {
+  const int lane = threadIdx.x & 31;
+  for (int64_t v = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; v < n;
+       v += (gridDim.x * (int64_t)blockDim.x) >> 5) {
+    const int f = node_first[v], c = node_ntiles[v];
+    for (int k = lane; k < c; k += 32) tile_node[f + k] = (int)v;
   }
 }
 
@@ -418,12 +440,16 @@ __global__ void build_positions_kernel(const int64_t *list_off, const int *list_
 
 }  // namespace
 
+// Defaults measured on the 264k-vertex road graph (one warp per tile):
+// narrow levels (the chain-like top of the tree, on the critical path) cut a
+// node into 32-column x 4-member tiles once m*d exceeds 1,024; wide levels
+// use 32 x 16 above 4,096; separators above 256 members always split.
 TilePolicy::TilePolicy() {
   for (int w = 0; w < kWidth; w++)
     for (int b = 0; b < kSep; b++) {
-      small_work[w][b] = b == kSep - 1 ? 0 : 1 << 16;  // separators above 256 members are always split
-      col_block[w][b] = 128;
-      sep_chunk[w][b] = 32;
+      small_work[w][b] = b == kSep - 1 ? 0 : (w == 0 ? 1024 : 4096);
+      col_block[w][b] = 32;
+      sep_chunk[w][b] = w == 0 ? 4 : 16;
     }
 }
 
@@ -641,10 +667,10 @@ void FillPlan::build_tiles(const TilePolicy &pol) {
   GH_CHECK(ntiles < INT32_MAX, H2H_ERR_ARG, "too many fill tiles");
   max_u = *std::max_element(mu.begin(), mu.end());
   max_c = *std::max_element(mc.begin(), mc.end());
-  // pass 2: node, c0, c1, u0, u1 per tile, then tiles per node
-  std::vector<int> host((size_t)(5 * ntiles + N));
-  int *tn = host.data(), *tc0 = tn + ntiles, *tc1 = tn + 2 * ntiles, *tu0 = tn + 3 * ntiles,
-      *tu1 = tn + 4 * ntiles, *nt = tn + 5 * ntiles;
+  // pass 2: per node its first ticket, tile count and tile shape; the
+  // ticket -> node array is expanded on the device
+  std::vector<int> host((size_t)4 * N);
+  int *nfirst = host.data(), *nt = nfirst + N, *ncb = nfirst + 2 * N, *nsc = nfirst + 3 * N;
   pool.parallel_for(K, 1, [&](int64_t lo, int64_t hi, int) {
     for (int64_t i = lo; i < hi; i++) {
       const Graph &g = *gs[i];
@@ -657,22 +683,17 @@ void FillPlan::build_tiles(const TilePolicy &pol) {
           const int v = g.tree_bfs[q], V = vb + v, d = g.depth[v];
           const int m = (int)(g.pos_hash[v + 1] - g.pos_hash[v]) - 1;
           int nt_node, cb, sc;
-          if (tiles_of(wb, m, d, nt_node, cb, sc)) {
-            tn[t] = V; tc0[t] = 0; tc1[t] = d; tu0[t] = 0; tu1[t] = m;
-            t++;
-          } else {
-            for (int c = 0; c < d; c += cb)
-              for (int u = 0; u < std::max(m, 1); u += sc) {
-                tn[t] = V; tc0[t] = c; tc1[t] = std::min(d, c + cb); tu0[t] = u; tu1[t] = std::min(m, u + sc);
-                t++;
-              }
-          }
+          tiles_of(wb, m, d, nt_node, cb, sc);
+          nfirst[V] = (int)t;
           nt[V] = nt_node;
+          ncb[V] = cb;
+          nsc[V] = sc;
+          t += nt_node;
         }
       }
     }
   });
-  const int64_t need = 5 * ntiles + N;
+  const int64_t need = ntiles + 4 * (int64_t)N;
   if (need > tiles_cap) {
     cudaFree(tiles);
     tiles = nullptr;
@@ -680,9 +701,13 @@ void FillPlan::build_tiles(const TilePolicy &pol) {
     tiles = dalloc<int>(need, work_bytes);
     tiles_cap = need;
   }
-  GH_CUDA(cudaMemcpy(tiles, host.data(), sizeof(int) * need, cudaMemcpyHostToDevice));
+  GH_CUDA(cudaMemcpy(tiles + ntiles, host.data(), sizeof(int) * 4 * (int64_t)N, cudaMemcpyHostToDevice));
+  expand_tiles_kernel<<<std::max(1, std::min(8192, (N * 32 + 255) / 256)), 256>>>(tiles + ntiles, tiles + ntiles + N,
+                                                                                  tiles, N);
+  GH_CUDA(cudaGetLastError());
   const int smem_dyn = enable_max_dynamic_smem(fill_flow_kernel);
-  smem = (size_t)max_u * 16 + (size_t)std::max(max_segs, 1) * 8;
+  // one staging slice per warp (4 warps per 128-thread block)
+  smem = 4 * ((size_t)((max_u + 1) & ~1) * 16 + (size_t)((std::max(max_segs, 1) + 1) & ~1) * 8);
   GH_CHECK(smem <= (size_t)smem_dyn, H2H_ERR_DEVICE, "separator or tree too large for the fill staging");
   int per_sm = 0;
   GH_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fill_flow_kernel, threads, smem));
@@ -702,12 +727,11 @@ void FillPlan::enqueue(cudaStream_t s, cudaEvent_t *fill_ev) {
   GH_CUDA(cudaMemsetAsync(err, 0, sizeof(int), s));
   FlowArgs A;
   A.tile_node = tiles;
-  A.tile_c0 = tiles + ntiles;
-  A.tile_c1 = tiles + 2 * ntiles;
-  A.tile_u0 = tiles + 3 * ntiles;
-  A.tile_u1 = tiles + 4 * ntiles;
   A.ntiles = (int)ntiles;
-  A.node_ntiles = tiles + 5 * ntiles;
+  A.node_first = tiles + ntiles;
+  A.node_ntiles = tiles + ntiles + N;
+  A.node_cb = tiles + ntiles + 2 * (int64_t)N;
+  A.node_sc = tiles + ntiles + 3 * (int64_t)N;
   A.node_cnt = done + N;
   A.father = father;
   A.depth = depth;
@@ -827,8 +851,8 @@ std::string tile_policy_tune(FillPlan &plan, ElimPlan &elim, cudaStream_t s, int
     }
     return best;
   };
-  static const int kSmall[] = {0, 1 << 12, 1 << 14, 1 << 16, 1 << 18};
-  static const int kShape[][2] = {{64, 16}, {128, 16}, {128, 32}, {256, 32}, {128, 64}, {256, 64}};
+  static const int kSmall[] = {0, 1 << 8, 1 << 10, 1 << 12, 1 << 14, 1 << 16};
+  static const int kShape[][2] = {{32, 4}, {32, 8}, {32, 16}, {32, 32}, {64, 16}, {64, 32}};
   TilePolicy best = plan.policy;
   float best_ms = 0;
   try {
