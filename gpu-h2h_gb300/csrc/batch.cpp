@@ -177,7 +177,7 @@ int h2h_batch_build(h2h_graph *const *graphs, int count, int threads, h2h_batch 
     clk.reset();
     gh::TilePolicy pol;
     if (const char *e = std::getenv("GPUH2H_TILE_POLICY"))
-      GH_CHECK(pol.parse(e), H2H_ERR_ARG, "GPUH2H_TILE_POLICY: expected 8 entries small_work/col_block/sep_chunk");
+      GH_CHECK(pol.parse(e), H2H_ERR_ARG, "GPUH2H_TILE_POLICY: expected 12 entries small_work/col_block/sep_chunk");
     b->fill = std::make_unique<gh::FillPlan>(b->gs, pol, b->elim->lists);
     GH_CUDA(cudaDeviceSynchronize());
     b->info.t_fill_plan_us = clk.us();
@@ -255,7 +255,7 @@ int h2h_batch_set_policy(h2h_batch *b, const char *policy) {
   if (!b || !policy) { gh::set_last_error("null batch or policy"); return H2H_ERR_ARG; }
   return gh::guarded([&] {
     gh::TilePolicy p;
-    GH_CHECK(p.parse(policy), H2H_ERR_ARG, "policy: expected 8 entries small_work/col_block/sep_chunk");
+    GH_CHECK(p.parse(policy), H2H_ERR_ARG, "policy: expected 12 entries small_work/col_block/sep_chunk");
     GH_CUDA(cudaStreamSynchronize(b->stream));
     b->drop_graph();
     b->fill->build_tiles(p);

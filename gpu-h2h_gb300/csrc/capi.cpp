@@ -314,7 +314,7 @@ int h2h_copy_adj(const h2h_graph *h, int64_t *adj_hash, int *adj_id, int *adj_w)
       gh::download_lists(gm);  // the lists live on the device
       if (adj_id) std::copy(g.x_id.begin(), g.x_id.end(), adj_id);
       if (adj_w) std::copy(g.x_w.begin(), g.x_w.end(), adj_w);
-      if (g.label_mode != H2H_LABEL_L3) {
+      if (!gh::uses_level_fill(g)) {
         std::vector<int>().swap(gm.x_id);
         std::vector<int>().swap(gm.x_w);
       }

@@ -3,6 +3,7 @@
 #pragma once
 
 #include <cstdint>
+#include <cstdlib>
 #include <memory>
 #include <string>
 #include <vector>
@@ -180,13 +181,14 @@ struct ElimPlan {
   void set_weights(int gi, const int *w, cudaStream_t s);  // arc weights in the graph's file order
 };
 
-// Tile shapes of the L4 dataflow fill, keyed on the width of the node's
-// tree level (below / at least the SM count) and its separator size m
-// (buckets m <= 16, <= 64, <= 256, > 256).  A node whose m * d is at most
-// small_work is one tile; a larger one is cut into col_block columns x
-// sep_chunk separator members.
+// Tile shapes of the L4 dataflow fill, keyed on the node's tree level --
+// class 0: fewer nodes than SMs (the chain-like top, on the critical path);
+// class 1: wider; class 2: wider and heavy (the level's min-plus work sum
+// m*d is at least 2^17 per SM) -- and on its separator size m (buckets m <= 16, <= 64,
+// <= 256, > 256).  A node whose m * d is at most small_work is one tile; a
+// larger one is cut into col_block columns x sep_chunk separator members.
 struct TilePolicy {
-  static constexpr int kWidth = 2, kSep = 4;
+  static constexpr int kWidth = 3, kSep = 4;
   int small_work[kWidth][kSep], col_block[kWidth][kSep], sep_chunk[kWidth][kSep];
   TilePolicy();
   static int sep_bucket(int m) { return m <= 16 ? 0 : m <= 64 ? 1 : m <= 256 ? 2 : 3; }
@@ -213,7 +215,7 @@ struct FillPlan {
   int *hld = nullptr, *htop = nullptr, *hpos = nullptr, *seg_top = nullptr, *seg_pos = nullptr;
   int64_t *seg_off = nullptr;
   int *done = nullptr, *next = nullptr, *err = nullptr, *tiles = nullptr;
-  int64_t ntiles = 0, tiles_cap = 0;
+  int64_t ntiles = 0, tiles_cap = 0, nchunks = 0;
   int max_u = 1, max_c = 1, max_segs = 1, blocks = 1, threads = 128;
   size_t smem = 0;
   int nsm = 0;
@@ -225,6 +227,7 @@ struct FillPlan {
   FillPlan(const FillPlan &) = delete;
   FillPlan &operator=(const FillPlan &) = delete;
   void build_tiles(const TilePolicy &pol);
+  std::vector<int> level_classes() const;  // TilePolicy class per forest level
   // Gathers the shortcut weights of the pos entries from the lists, resets
   // rows and flags and runs the fill on s.
   void enqueue(cudaStream_t s, cudaEvent_t *fill_ev = nullptr);
@@ -249,6 +252,11 @@ inline void build_tree_and_rmq(Graph &g) {
 }
 void allocate_labels_and_bfs(Graph &g);                // tree.cpp
 void fill_labels_gpu(Graph &g);                        // labels.cu
+// The level-synchronous fill (L3 labels, or L4 with GPUH2H_LEVEL_FILL set)
+// runs from host position lists; the L4 dataflow fill builds them on the GPU.
+inline bool uses_level_fill(const Graph &g) {
+  return g.label_mode == H2H_LABEL_L3 || std::getenv("GPUH2H_LEVEL_FILL") != nullptr;
+}
 void download_labels(const Graph &g, int *dis_out);    // labels.cu, reference layout
 // labels.cu: the graph's position lists (reference layout, graph-local ids)
 void download_positions(const Graph &g, int *pos_id, int *pos_pos);

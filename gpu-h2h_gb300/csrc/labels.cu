@@ -207,6 +207,10 @@ struct FlowArgs {
   const int *tile_node;
   int ntiles;
   const int *node_first, *node_ntiles, *node_cb, *node_sc;
+  // the counter hands out chunks of consecutive tickets: one tile on the
+  // narrow levels, several on the wide ones (fewer atomics)
+  const int *chunk_start;  // [nchunks + 1]
+  int nchunks;
   int *node_cnt;           // finished tiles per node
   const int *father;
   const int *depth;
@@ -257,10 +261,12 @@ __global__ void __launch_bounds__(128) fill_flow_kernel(FlowArgs A) {
   int *s_top = xs_w + ual;                           // [max_segs]
   int *s_pos = s_top + sal;                          // [max_segs]
   for (;;) {
-    int t = 0;
-    if (lane == 0) t = atomicAdd(A.next, 1);
-    t = __shfl_sync(0xffffffffu, t, 0);
-    if (t >= A.ntiles) return;
+    int k = 0;
+    if (lane == 0) k = atomicAdd(A.next, 1);
+    k = __shfl_sync(0xffffffffu, k, 0);
+    if (k >= A.nchunks) return;
+    const int t_end = min(__ldg(A.chunk_start + k + 1), A.ntiles);
+    for (int t = max(__ldg(A.chunk_start + k), 0); t < t_end; t++) {
     const int v = __ldg(A.tile_node + t);
     const int d = __ldg(A.depth + v);
     const int f = __ldg(A.father + v);
@@ -276,6 +282,7 @@ __global__ void __launch_bounds__(128) fill_flow_kernel(FlowArgs A) {
     const bool whole_sep = u0 == 0 && u1 == m;                  // this tile sees every member
     const int nu = u1 - u0;
     // separator entries and root-path segments need no finished row
+#pragma unroll 4
     for (int i = lane; i < nu; i += 32) {
       xs_p[i] = __ldg(A.pos_pos + pb + u0 + i);
       xs_w[i] = __ldg(A.pos_w + pb + u0 + i);
@@ -338,6 +345,7 @@ __global__ void __launch_bounds__(128) fill_flow_kernel(FlowArgs A) {
       }
     }
     __syncwarp();  // the slice is restaged only after every lane left the sweep
+    }
   }
 }
 
@@ -440,16 +448,19 @@ __global__ void build_positions_kernel(const int64_t *list_off, const int *list_
 
 }  // namespace
 
-// Defaults measured on the 264k-vertex road graph (one warp per tile):
-// narrow levels (the chain-like top of the tree, on the critical path) cut a
-// node into 32-column x 4-member tiles once m*d exceeds 1,024; wide levels
-// use 32 x 16 above 4,096; separators above 256 members always split.
+// Defaults measured on road graphs (one warp per tile): narrow levels cut a
+// node into 32-column x 4-member tiles once m*d exceeds 1,024 (the 264k-
+// vertex graph's fill is a latency chain through 1,343 such levels); wider
+// levels 32 x 16 above 4,096; heavy levels (the 6.26M-vertex graph's middle)
+// 128 x 256 above 16,384 -- whole separators, so no atomicMin combining.
+// Separators above 256 members always split.
 TilePolicy::TilePolicy() {
+  static const int sw[kWidth] = {1024, 4096, 16384}, cb[kWidth] = {32, 32, 128}, sc[kWidth] = {4, 16, 256};
   for (int w = 0; w < kWidth; w++)
     for (int b = 0; b < kSep; b++) {
-      small_work[w][b] = b == kSep - 1 ? 0 : (w == 0 ? 1024 : 4096);
-      col_block[w][b] = 32;
-      sep_chunk[w][b] = w == 0 ? 4 : 16;
+      small_work[w][b] = b == kSep - 1 ? 0 : sw[w];
+      col_block[w][b] = cb[w];
+      sep_chunk[w][b] = sc[w];
     }
 }
 
@@ -603,6 +614,29 @@ void FillPlan::release_work() {
   seg_off = nullptr;
 }
 
+std::vector<int> FillPlan::level_classes() const {
+  int nlev = 0;
+  for (const Graph *g : gs) nlev = std::max(nlev, (int)g->tree_hash.size() - 1);
+  std::vector<int64_t> width(nlev, 0), work(nlev, 0);
+  for (const Graph *g : gs)
+    for (int l = 0; l + 1 < (int)g->tree_hash.size(); l++) {
+      width[l] += g->tree_hash[l + 1] - g->tree_hash[l];
+      for (int q = g->tree_hash[l]; q < g->tree_hash[l + 1]; q++) {
+        const int v = g->tree_bfs[q];
+        work[l] += (g->pos_hash[v + 1] - g->pos_hash[v] - 1) * (int64_t)g->depth[v];
+      }
+    }
+  // narrow: fewer nodes than SMs, whatever their work (the critical path);
+  // heavy: a wider level with at least 2^17 min-plus updates per SM
+  // (GPUH2H_HEAVY_LEVEL_WORK overrides the per-SM figure)
+  int64_t per_sm = int64_t(1) << 17;
+  if (const char *e = std::getenv("GPUH2H_HEAVY_LEVEL_WORK")) per_sm = std::max(1LL, std::atoll(e));
+  std::vector<int> cls(nlev, 0);
+  for (int l = 0; l < nlev; l++)
+    cls[l] = width[l] < nsm ? 0 : work[l] >= (int64_t)nsm * per_sm ? 2 : 1;
+  return cls;
+}
+
 // Tiles in forest BFS order (level l of every graph, then level l + 1): a
 // node's father always holds an earlier ticket, so the dataflow cannot wait
 // on work no CTA has taken.  Two passes over the graphs in parallel: tile
@@ -613,9 +647,7 @@ void FillPlan::build_tiles(const TilePolicy &pol) {
   const int K = (int)gs.size();
   int nlev = 0;
   for (const Graph *g : gs) nlev = std::max(nlev, (int)g->tree_hash.size() - 1);
-  std::vector<int64_t> width(nlev, 0);
-  for (const Graph *g : gs)
-    for (int l = 0; l + 1 < (int)g->tree_hash.size(); l++) width[l] += g->tree_hash[l + 1] - g->tree_hash[l];
+  const std::vector<int> lcls = level_classes();
   auto tiles_of = [&](int wb, int m, int d, int &nt_node, int &cb, int &sc) {
     const int sb = TilePolicy::sep_bucket(m);
     if ((int64_t)m * d <= pol.small_work[wb][sb]) {
@@ -641,7 +673,7 @@ void FillPlan::build_tiles(const TilePolicy &pol) {
       const int gl = (int)g.tree_hash.size() - 1;
       cnt[i].assign(gl, 0);
       for (int l = 0; l < gl; l++) {
-        const int wb = width[l] >= nsm ? 1 : 0;
+        const int wb = lcls[l];
         for (int q = g.tree_hash[l]; q < g.tree_hash[l + 1]; q++) {
           const int v = g.tree_bfs[q], d = g.depth[v];
           const int m = (int)(g.pos_hash[v + 1] - g.pos_hash[v]) - 1;
@@ -677,7 +709,7 @@ void FillPlan::build_tiles(const TilePolicy &pol) {
       const int vb = vbase[i];
       const int gl = (int)g.tree_hash.size() - 1;
       for (int l = 0; l < gl; l++) {
-        const int wb = width[l] >= nsm ? 1 : 0;
+        const int wb = lcls[l];
         int64_t t = off[i][l];
         for (int q = g.tree_hash[l]; q < g.tree_hash[l + 1]; q++) {
           const int v = g.tree_bfs[q], V = vb + v, d = g.depth[v];
@@ -693,7 +725,7 @@ void FillPlan::build_tiles(const TilePolicy &pol) {
       }
     }
   });
-  const int64_t need = ntiles + 4 * (int64_t)N;
+  const int64_t need = ntiles + 4 * (int64_t)N + (int64_t)(ntiles + nlev + 1);  // + chunk table bound
   if (need > tiles_cap) {
     cudaFree(tiles);
     tiles = nullptr;
@@ -701,7 +733,32 @@ void FillPlan::build_tiles(const TilePolicy &pol) {
     tiles = dalloc<int>(need, work_bytes);
     tiles_cap = need;
   }
+  // chunks: forest levels in ticket order.  A level with many times more
+  // tiles than resident warps hands them out in groups (fewer atomics on the
+  // counter); any other level one by one, so its tiles spread over warps.
+  std::vector<int> chunks;
+  chunks.reserve((size_t)(ntiles / 2 + 1024));
+  {
+    const int64_t warps = (int64_t)nsm * 64;
+    int64_t t = 0;
+    for (int l = 0; l < nlev; l++) {
+      int64_t lt = 0;
+      for (int i = 0; i < K; i++)
+        if (l < (int)cnt[i].size()) lt += cnt[i][l];
+      const int step = (int)std::max<int64_t>(1, std::min<int64_t>(8, lt / (8 * warps)));
+      const int64_t e = t + lt;  // this level's tickets are [t, e)
+      for (int64_t c = t; c < e; c += step) chunks.push_back((int)c);
+      t = e;
+    }
+    GH_CHECK(t == ntiles, H2H_ERR_STATE, "fill chunks do not cover the tiles");
+    chunks.push_back((int)ntiles);
+  }
+  for (size_t c = 1; c < chunks.size(); c++)
+    GH_CHECK(chunks[c - 1] < chunks[c], H2H_ERR_STATE, "fill chunk table out of order");
+  nchunks = (int64_t)chunks.size() - 1;
   GH_CUDA(cudaMemcpy(tiles + ntiles, host.data(), sizeof(int) * 4 * (int64_t)N, cudaMemcpyHostToDevice));
+  GH_CUDA(cudaMemcpy(tiles + ntiles + 4 * (int64_t)N, chunks.data(), sizeof(int) * chunks.size(),
+                     cudaMemcpyHostToDevice));
   expand_tiles_kernel<<<std::max(1, std::min(8192, (N * 32 + 255) / 256)), 256>>>(tiles + ntiles, tiles + ntiles + N,
                                                                                   tiles, N);
   GH_CUDA(cudaGetLastError());
@@ -732,6 +789,8 @@ void FillPlan::enqueue(cudaStream_t s, cudaEvent_t *fill_ev) {
   A.node_ntiles = tiles + ntiles + N;
   A.node_cb = tiles + ntiles + 2 * (int64_t)N;
   A.node_sc = tiles + ntiles + 3 * (int64_t)N;
+  A.chunk_start = tiles + ntiles + 4 * (int64_t)N;
+  A.nchunks = (int)nchunks;
   A.node_cnt = done + N;
   A.father = father;
   A.depth = depth;
@@ -816,21 +875,13 @@ void FillPlan::attach(bool first) {
 std::string tile_policy_tune(FillPlan &plan, ElimPlan &elim, cudaStream_t s, int rounds) {
   bool used[TilePolicy::kWidth][TilePolicy::kSep] = {};
   {
-    int nlev = 0;
-    for (const Graph *g : plan.gs) nlev = std::max(nlev, (int)g->tree_hash.size() - 1);
-    for (int l = 0; l < nlev; l++) {
-      int64_t width = 0;
-      for (const Graph *g : plan.gs)
-        if (l + 1 < (int)g->tree_hash.size()) width += g->tree_hash[l + 1] - g->tree_hash[l];
-      const int wb = width >= plan.nsm ? 1 : 0;
-      for (const Graph *g : plan.gs) {
-        if (l + 1 >= (int)g->tree_hash.size()) continue;
+    const std::vector<int> lcls = plan.level_classes();
+    for (const Graph *g : plan.gs)
+      for (int l = 0; l + 1 < (int)g->tree_hash.size(); l++)
         for (int q = g->tree_hash[l]; q < g->tree_hash[l + 1]; q++) {
           const int v = g->tree_bfs[q];
-          used[wb][TilePolicy::sep_bucket((int)(g->pos_hash[v + 1] - g->pos_hash[v]) - 1)] = true;
+          used[lcls[l]][TilePolicy::sep_bucket((int)(g->pos_hash[v + 1] - g->pos_hash[v]) - 1)] = true;
         }
-      }
-    }
   }
   cudaEvent_t ev[2];
   GH_CUDA(cudaEventCreate(&ev[0]));
@@ -852,7 +903,7 @@ std::string tile_policy_tune(FillPlan &plan, ElimPlan &elim, cudaStream_t s, int
     return best;
   };
   static const int kSmall[] = {0, 1 << 8, 1 << 10, 1 << 12, 1 << 14, 1 << 16};
-  static const int kShape[][2] = {{32, 4}, {32, 8}, {32, 16}, {32, 32}, {64, 16}, {64, 32}};
+  static const int kShape[][2] = {{32, 4}, {32, 8}, {32, 16}, {32, 32}, {64, 32}, {128, 256}};
   TilePolicy best = plan.policy;
   float best_ms = 0;
   try {
@@ -894,11 +945,11 @@ void fill_labels_gpu(Graph &g) {
   DeviceIndex &D = g.dev;
   // L4 runs as a dataflow over the tree; L3 (order-dependent, as shipped)
   // keeps the level-synchronous kernel that applies the reference's order.
-  const bool flow = g.label_mode == H2H_LABEL_L4 && !std::getenv("GPUH2H_LEVEL_FILL");
+  const bool flow = !uses_level_fill(g);
   if (flow) {
     TilePolicy pol;
     if (const char *e = std::getenv("GPUH2H_TILE_POLICY"))
-      GH_CHECK(pol.parse(e), H2H_ERR_ARG, "GPUH2H_TILE_POLICY: expected 8 entries small_work/col_block/sep_chunk");
+      GH_CHECK(pol.parse(e), H2H_ERR_ARG, "GPUH2H_TILE_POLICY: expected 12 entries small_work/col_block/sep_chunk");
     FillPlan plan({&g}, pol, D.lists);
     GH_CUDA(cudaDeviceSynchronize());
     g.t.translate_labels = clk.us();

@@ -82,9 +82,9 @@ void allocate_labels_and_bfs(Graph &g) {
     g.dis_hash[v + 1] = g.dis_hash[v] + g.depth[v];
     g.pos_hash[v + 1] = g.pos_hash[v] + (g.x_off[v + 1] - g.x_off[v]) + 1;
   }
-  // host position lists only for L3 (its level fill runs from them); L4
-  // builds them on the GPU from the device lists
-  if (g.label_mode == H2H_LABEL_L3) {
+  // host position lists only for the level-synchronous fill; the dataflow
+  // fill builds them on the GPU from the device lists
+  if (uses_level_fill(g)) {
     if ((int64_t)g.x_id.size() != g.x_off[n]) download_lists(g);
     g.pos_id.resize(g.pos_hash[n]);
     g.pos_pos.resize(g.pos_hash[n]);

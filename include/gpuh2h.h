@@ -191,9 +191,10 @@ int h2h_batch_rebuild(h2h_batch *b);
 /* Waits for the batch's stream.  Accessors (h2h_copy_adj, h2h_copy_labels)
  * read the device arrays, so they see the last rebuild once it returned. */
 int h2h_batch_sync_host(h2h_batch *b);
-/* Tile shapes of the forest label fill.  policy is 8 entries
- * "small_work/col_block/sep_chunk" separated by spaces: level width below /
- * at least the SM count, times separator size m <= 16, <= 64, <= 256, > 256.
+/* Tile shapes of the forest label fill.  policy is 12 entries
+ * "small_work/col_block/sep_chunk" separated by spaces: level class (fewer
+ * nodes than SMs / wider / heavy: at least 2^17 min-plus updates per SM),
+ * times separator size m <= 16, <= 64, <= 256, > 256.
  * h2h_batch_tune times candidate shapes on this batch (coordinate descent,
  * `rounds` passes), keeps the fastest and writes it to policy_out. */
 int h2h_batch_set_policy(h2h_batch *b, const char *policy);

@@ -132,11 +132,11 @@ def test_tuned_policy_keeps_labels(batch_specs):
     ref = [g.labels()["dis"] for g in graphs]
     default = b.policy()
     pol = b.tune(1)
-    assert pol == b.policy() and len(pol.split()) == 8
+    assert pol == b.policy() and len(pol.split()) == 12
     for g, d in zip(graphs, ref):
         assert np.array_equal(g.labels()["dis"], d)
     # a hand-set policy that splits every node finely
-    b.set_policy(" ".join(["0/32/8"] * 8))
+    b.set_policy(" ".join(["0/32/8"] * 12))
     b.rebuild()
     for g, d in zip(graphs, ref):
         assert np.array_equal(g.labels()["dis"], d)

@@ -158,3 +158,33 @@ def test_global_merge_staging(cfg0_root, golden0, monkeypatch):
         g = build(gpuh2h.files_for(cfg0_root, "cfg0"), 6, C)
         assert np.array_equal(g.order(), golden0[tag + "order"])
         assert np.array_equal(_sha(g.labels()["dis"]), golden0[tag + "sha256/dis"])
+
+
+@pytest.mark.parametrize("env", ["GPUH2H_CLUSTER_HEAP", "GPUH2H_LEVEL_FILL"])
+def test_alternate_kernels(cfg0_root, golden0, monkeypatch, env):
+    """The global order on one thread-block cluster (instead of every SM) and
+    the level-synchronous L4 fill (instead of the dataflow) give the same
+    order, adjacency, labels and answers."""
+    import gpuh2h
+    monkeypatch.setenv(env, "1")
+    for C in (1, 2, 6):
+        tag = "cfg0_C%d_L4/" % C
+        g = build(gpuh2h.files_for(cfg0_root, "cfg0"), 6, C)
+        assert np.array_equal(g.order(), golden0[tag + "order"])
+        ah, aid, aw = g.adj()
+        assert np.array_equal(_sha(aw), golden0[tag + "sha256/adj_w"])
+        assert np.array_equal(_sha(g.labels()["dis"]), golden0[tag + "sha256/dis"])
+        pairs = golden0["pairs"]
+        assert np.array_equal(g.query(pairs[:, 0], pairs[:, 1], gpuh2h.QUERY_LCA), golden0[tag + "q_lca"])
+
+
+@pytest.mark.parametrize("policy", [" ".join(["0/32/4"] * 12),
+                                    "65536/64/32 65536/64/32 65536/64/32 0/64/32 "
+                                    "262144/32/16 262144/32/16 262144/32/16 0/32/16 "
+                                    "0/128/256 0/128/256 0/128/256 0/128/256"])
+def test_tile_policies(cfg0_root, golden0, monkeypatch, policy):
+    """Any tile shape of the dataflow fill gives the same labels."""
+    import gpuh2h
+    monkeypatch.setenv("GPUH2H_TILE_POLICY", policy)
+    g = build(gpuh2h.files_for(cfg0_root, "cfg0"), 6, 2)
+    assert np.array_equal(_sha(g.labels()["dis"]), golden0["cfg0_C2_L4/sha256/dis"])
