@@ -401,6 +401,10 @@ int h2h_gen_uniform_pairs(int n_vertices, int64_t n, uint64_t seed, int *x, int 
 
 int h2h_gen_local_pairs(const h2h_graph *h, int64_t n, int max_hops, uint64_t seed, int *x, int *y) {
   if (!h || n < 0 || (n > 0 && (!x || !y))) { gh::set_last_error("bad argument"); return H2H_ERR_ARG; }
+  if ((int)h->g.adj_off.size() != h->g.n + 1 || h->g.n == 0) {
+    gh::set_last_error("the input arcs are not loaded (an index read by h2h_load_index has none)");
+    return H2H_ERR_STATE;
+  }
   gh::gen_local_pairs(h->g, n, max_hops, seed, x, y);
   return H2H_OK;
 }

@@ -1302,6 +1302,26 @@ void ElimPlan::enqueue_gather(cudaStream_t s) {
   GH_CUDA(cudaGetLastError());
 }
 
+ListStore upload_lists(const std::vector<int64_t> &off, const std::vector<int> &id, const std::vector<int> &w) {
+  ListStore L;
+  auto la = std::make_shared<ListArrays>();
+  const int64_t t = off.empty() ? 0 : off.back();
+  la->off = dalloc<int64_t>(std::max<size_t>(off.size(), 1));
+  la->id = dalloc<int>(std::max<int64_t>(t, 1));
+  la->w = dalloc<int>(std::max<int64_t>(t, 1));
+  L.off = la->off;
+  L.id = la->id;
+  L.w = la->w;
+  L.total = t;
+  L.keep = la;
+  if (!off.empty()) GH_CUDA(cudaMemcpy(L.off, off.data(), sizeof(int64_t) * off.size(), cudaMemcpyHostToDevice));
+  if (t) {
+    GH_CUDA(cudaMemcpy(L.id, id.data(), sizeof(int) * t, cudaMemcpyHostToDevice));
+    GH_CUDA(cudaMemcpy(L.w, w.data(), sizeof(int) * t, cudaMemcpyHostToDevice));
+  }
+  return L;
+}
+
 void download_lists(Graph &g) {
   const ListStore &L = g.dev.lists;
   GH_CHECK(L.id && (int64_t)g.x_off.size() == g.n + 1, H2H_ERR_STATE, "not contracted");

@@ -262,6 +262,14 @@ void download_labels(const Graph &g, int *dis_out);    // labels.cu, reference l
 void download_positions(const Graph &g, int *pos_id, int *pos_pos);
 // contract.cu: host copies of the X lists (graph-local ids) from the device
 void download_lists(Graph &g);
+// Device copies of a saved index (index_io.cpp loads the file):
+ListStore upload_lists(const std::vector<int64_t> &off, const std::vector<int> &id,
+                       const std::vector<int> &w);                         // contract.cu
+void upload_rmq(Graph &g, const std::vector<int64_t> &rmq_hash, const std::vector<int> &rmq_id);  // query.cu
+// labels.cu: rows (reference layout, dis_hash offsets) into padded device
+// rows plus the position arrays; sets drow_host and the DeviceIndex
+void upload_labels(Graph &g, const std::vector<int> &dis, const std::vector<int> &pos_id,
+                   const std::vector<int> &pos_pos);
 void upload_query_index(Graph &g);                     // query.cu
 // query.cu; bad: the flag word set when a pair holds an id out of range
 // (nullptr: the graph's own)

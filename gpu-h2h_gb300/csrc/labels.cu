@@ -1078,6 +1078,62 @@ void fill_labels_gpu(Graph &g) {
 }
 
 // Copies the filled labels back into the reference's unpadded layout.
+void upload_labels(Graph &g, const std::vector<int> &dis, const std::vector<int> &pos_id,
+                   const std::vector<int> &pos_pos) {
+  const int n = g.n;
+  DeviceIndex &D = g.dev;
+  D.release_labels();
+  D.n = n;
+  D.pos_base = 0;
+  std::vector<int64_t> drow(n + 1, 0);
+  for (int v = 0; v < n; v++) drow[v + 1] = drow[v] + ((g.depth[v] + 3) & ~3);
+  D.dis_padded = drow[n];
+  D.pos = g.pos_hash[n];
+  D.drow = dalloc_owned<int64_t>(n + 1, D);
+  D.dis = dalloc_owned<int>(D.dis_padded, D);
+  D.pos_hash = dalloc_owned<int64_t>(n + 1, D);
+  D.pos_pos = dalloc_owned<int>(D.pos, D);
+  D.pos_id = dalloc_owned<int>(D.pos, D);
+  D.father = dalloc_owned<int>(n, D);
+  D.depth = dalloc_owned<int>(n, D);
+  D.err = dalloc_owned<int>(1, D);
+  GH_CUDA(cudaMemcpy(D.drow, drow.data(), sizeof(int64_t) * (n + 1), cudaMemcpyHostToDevice));
+  GH_CUDA(cudaMemcpy(D.pos_hash, g.pos_hash.data(), sizeof(int64_t) * (n + 1), cudaMemcpyHostToDevice));
+  if (D.pos) {
+    GH_CUDA(cudaMemcpy(D.pos_pos, pos_pos.data(), sizeof(int) * D.pos, cudaMemcpyHostToDevice));
+    GH_CUDA(cudaMemcpy(D.pos_id, pos_id.data(), sizeof(int) * D.pos, cudaMemcpyHostToDevice));
+  }
+  GH_CUDA(cudaMemcpy(D.father, g.father.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
+  GH_CUDA(cudaMemcpy(D.depth, g.depth.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
+  GH_CUDA(cudaMemset(D.err, 0, sizeof(int)));
+  // rows into the padded layout through a page-locked staging buffer of at
+  // most 64 Mi entries (padding entries are INT_MAX, as the fill leaves them)
+  const int64_t kStage = int64_t(1) << 26;
+  int *stage = nullptr;
+  GH_CUDA(cudaMallocHost(&stage, sizeof(int) * std::min<int64_t>(std::max<int64_t>(D.dis_padded, 1), kStage)));
+  try {
+    int v = 0;
+    while (v < n) {
+      const int64_t p0 = drow[v];
+      int w = v;
+      while (w < n && drow[w + 1] - p0 <= kStage) w++;
+      GH_CHECK(w > v, H2H_ERR_ARG, "a label row longer than the upload staging");
+      for (int u = v; u < w; u++) {
+        int *row = stage + (drow[u] - p0);
+        std::copy(dis.begin() + g.dis_hash[u], dis.begin() + g.dis_hash[u] + g.depth[u], row);
+        for (int64_t j = g.depth[u]; j < drow[u + 1] - drow[u]; j++) row[j] = INT_MAX;
+      }
+      GH_CUDA(cudaMemcpy(D.dis + p0, stage, sizeof(int) * (drow[w] - p0), cudaMemcpyHostToDevice));
+      v = w;
+    }
+  } catch (...) {
+    cudaFreeHost(stage);
+    throw;
+  }
+  cudaFreeHost(stage);
+  g.drow_host.swap(drow);
+}
+
 // Position lists in the reference layout with graph-local ids: the host
 // copies (L3) or the graph's range of the device arrays (L4).
 void download_positions(const Graph &g, int *pos_id, int *pos_pos) {

@@ -294,6 +294,26 @@ void build_rmq_gpu(const std::vector<Graph *> &gs) {
   }
 }
 
+void upload_rmq(Graph &g, const std::vector<int64_t> &rmq_hash, const std::vector<int> &rmq_id) {
+  DeviceIndex &D = g.dev;
+  for (void *p : D.owned_rmq) cudaFree(p);
+  D.owned_rmq.clear();
+  D.bytes -= D.rmq_bytes;
+  D.rmq_bytes = 0;
+  D.euler = g.euler_n;
+  D.rmq = g.rmq_total;
+  D.first = dalloc<int>(g.n, D.rmq_bytes);
+  D.owned_rmq.push_back(D.first);
+  D.rmq_hash = dalloc<int64_t>(D.euler, D.rmq_bytes);
+  D.owned_rmq.push_back(D.rmq_hash);
+  D.rmq_id = dalloc<int>(D.rmq, D.rmq_bytes);
+  D.owned_rmq.push_back(D.rmq_id);
+  D.bytes += D.rmq_bytes;
+  GH_CUDA(cudaMemcpy(D.first, g.first.data(), sizeof(int) * g.n, cudaMemcpyHostToDevice));
+  GH_CUDA(cudaMemcpy(D.rmq_hash, rmq_hash.data(), sizeof(int64_t) * D.euler, cudaMemcpyHostToDevice));
+  GH_CUDA(cudaMemcpy(D.rmq_id, rmq_id.data(), sizeof(int) * D.rmq, cudaMemcpyHostToDevice));
+}
+
 void download_rmq(const Graph &g, int64_t *rmq_hash, int *rmq_id) {
   GH_CHECK(g.dev.rmq_hash && g.dev.rmq_id, H2H_ERR_STATE, "sparse table not built");
   if (rmq_hash) GH_CUDA(cudaMemcpy(rmq_hash, g.dev.rmq_hash, sizeof(int64_t) * g.euler_n, cudaMemcpyDeviceToHost));

@@ -108,6 +108,8 @@ SIGNATURES = {
     "h2h_fill_labels_l4_noalloc": (_i32, [_i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i64, _vp, _i32, _i32,
                                           _vp]),
     "h2h_copy_input_arcs": (_i32, [_vp, _vp, _vp, _vp]),
+    "h2h_save_index": (_i32, [_vp, _cp]),
+    "h2h_load_index": (_i32, [_cp, C.POINTER(_vp)]),
     "h2h_batch_build": (_i32, [_vp, _i32, _i32, C.POINTER(_vp)]),
     "h2h_batch_set_weights": (_i32, [_vp, _i32, _vp]),
     "h2h_batch_rebuild": (_i32, [_vp]),
@@ -200,6 +202,21 @@ class Graph:
         _check(rc)
         self.h = h
         self.graphName = graphName
+
+    @classmethod
+    def load_index(cls, path: str, graphName: str = "index") -> "Graph":
+        """A built index read back from h2h_save_index's file (no rebuild)."""
+        L = load_library()
+        h = C.c_void_p()
+        _check(L.h2h_load_index(path.encode(), C.byref(h)))
+        g = cls.__new__(cls)
+        g._L = L
+        g.h = h
+        g.graphName = graphName
+        return g
+
+    def save_index(self, path: str):
+        _check(self._L.h2h_save_index(self.h, path.encode()))
 
     def close(self):
         if getattr(self, "h", None):

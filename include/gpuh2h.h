@@ -253,6 +253,17 @@ int h2h_server_reset_stats(h2h_server *s);
 /* Drains the queue, then stops the worker and frees the slots. */
 void h2h_server_free(h2h_server *s);
 
+/* The built index on disk, so a process (a server) restarts without a
+ * rebuild.  No counterpart in the reference, which rebuilds on every run.
+ * h2h_save_index writes the elimination order, tree, Euler tour and sparse
+ * table, X(v) lists, label and position arrays in the reference's layouts
+ * (a versioned binary format); h2h_load_index validates sizes, offsets and
+ * id ranges before it allocates on the GPU (H2H_ERR_FORMAT otherwise) and
+ * returns a handle that answers queries and serves every accessor; it has no
+ * input arcs (h2h_gen_local_pairs, h2h_batch_build need a loaded graph). */
+int h2h_save_index(const h2h_graph *g, const char *path);
+int h2h_load_index(const char *path, h2h_graph **out);
+
 /* The stored arcs of a loaded graph in CSR order (self-loops dropped,
  * parallel arcs kept, each vertex's arcs in Edge-file order):
  * adj_off[n+1], adj_v[m], adj_w[m]. */

@@ -154,3 +154,25 @@ def test_g2h_cli_argument_count_rule(tmp_path):
     for argv in ([], ["13"], ["13", "4", "1", "2", "1", "1", "2"]):
         r = subprocess.run([_build.CLI] + argv, cwd=str(tmp_path), capture_output=True, timeout=60)
         assert r.returncode == 0 and r.stdout == b"" and r.stderr == b""
+
+
+def test_index_file_validation(tmp_path):
+    """h2h_load_index rejects missing, foreign and truncated files before it
+    touches a GPU."""
+    import gpuh2h
+    L = gpuh2h.load_library()
+    h = C.c_void_p()
+    assert L.h2h_load_index(str(tmp_path / "none.idx").encode(), C.byref(h)) == -2
+    bad = tmp_path / "bad.idx"
+    bad.write_bytes(b"NOTANIDX" + b"\0" * 64)
+    assert L.h2h_load_index(str(bad).encode(), C.byref(h)) == -3
+    trunc = tmp_path / "trunc.idx"
+    trunc.write_bytes(b"GPUH2HIX" + (1).to_bytes(4, "little") + (16).to_bytes(4, "little") + b"\0" * 10)
+    assert L.h2h_load_index(str(trunc).encode(), C.byref(h)) == -3
+    # a header whose counts disagree (n = 5, euler_n = 3)
+    import struct
+    hdr = struct.pack("<9q8i", 5, 8, 3, 10, 4, 9, 15, 7, 9, 3, 1, 4, 0, 3, 5, 1, 3)
+    incons = tmp_path / "incons.idx"
+    incons.write_bytes(b"GPUH2HIX" + struct.pack("<II", 1, 16) + hdr + struct.pack("<I", 0))
+    assert L.h2h_load_index(str(incons).encode(), C.byref(h)) == -3
+    assert not h
