@@ -183,8 +183,8 @@ struct ElimPlan {
 
 // Tile shapes of the L4 dataflow fill, keyed on the node's tree level --
 // class 0: fewer nodes than SMs (the chain-like top, on the critical path);
-// class 1: wider; class 2: wider and heavy (the level's min-plus work sum
-// m*d is at least 2^17 per SM) -- and on its separator size m (buckets m <= 16, <= 64,
+// class 1: wider; class 2: wider and heavy (its nodes average at least 2^18
+// min-plus updates m*d) -- and on its separator size m (buckets m <= 16, <= 64,
 // <= 256, > 256).  A node whose m * d is at most small_work is one tile; a
 // larger one is cut into col_block columns x sep_chunk separator members.
 struct TilePolicy {

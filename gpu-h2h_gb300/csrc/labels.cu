@@ -21,6 +21,7 @@
 // u-row reads are 128-bit vector loads.
 #include <algorithm>
 #include <climits>
+#include <cstdio>
 #include <cstdlib>
 #include <sstream>
 
@@ -209,7 +210,7 @@ struct FlowArgs {
   const int *node_first, *node_ntiles, *node_cb, *node_sc;
   // the counter hands out chunks of consecutive tickets: one tile on the
   // narrow levels, several on the wide ones (fewer atomics)
-  const int *chunk_start;  // [nchunks + 1]
+  const int *chunk_start;  // [nchunks + 1]; nullptr: chunk k is tile k
   int nchunks;
   int *node_cnt;           // finished tiles per node
   const int *father;
@@ -265,8 +266,9 @@ __global__ void __launch_bounds__(128) fill_flow_kernel(FlowArgs A) {
     if (lane == 0) k = atomicAdd(A.next, 1);
     k = __shfl_sync(0xffffffffu, k, 0);
     if (k >= A.nchunks) return;
-    const int t_end = min(__ldg(A.chunk_start + k + 1), A.ntiles);
-    for (int t = max(__ldg(A.chunk_start + k), 0); t < t_end; t++) {
+    const int t_beg = A.chunk_start ? max(__ldg(A.chunk_start + k), 0) : k;
+    const int t_end = A.chunk_start ? min(__ldg(A.chunk_start + k + 1), A.ntiles) : k + 1;
+    for (int t = t_beg; t < t_end; t++) {
     const int v = __ldg(A.tile_node + t);
     const int d = __ldg(A.depth + v);
     const int f = __ldg(A.father + v);
@@ -493,6 +495,14 @@ bool TilePolicy::parse(const std::string &text) {
 
 FillPlan::FillPlan(const std::vector<Graph *> &graphs, const TilePolicy &pol, const ListStore &lst)
     : gs(graphs), policy(pol), lists(lst) {
+  const bool trace = std::getenv("GPUH2H_TRACE") != nullptr;
+  Clock tclk;
+  auto mark = [&](const char *what) {
+    if (!trace) return;
+    cudaDeviceSynchronize();
+    std::fprintf(stderr, "[gpuh2h] fill plan: %s %.3f ms\n", what, tclk.us() / 1e3);
+    tclk.reset();
+  };
   const int K = (int)gs.size();
   GH_CHECK(K >= 1, H2H_ERR_ARG, "no graph to label");
   vbase.assign(K, 0);
@@ -550,6 +560,7 @@ FillPlan::FillPlan(const std::vector<Graph *> &graphs, const TilePolicy &pol, co
   f_drow[N] = dis_total;
   f_pos_hash[N] = pos_total;
   f_seg_off[N] = seg_total;
+  mark("host assembly");
   threads = 128;
   int dev = 0;
   GH_CUDA(cudaGetDevice(&dev));
@@ -580,6 +591,7 @@ FillPlan::FillPlan(const std::vector<Graph *> &graphs, const TilePolicy &pol, co
     GH_CUDA(cudaMemcpy(father, f_father.data(), sizeof(int) * N, cudaMemcpyHostToDevice));
     GH_CUDA(cudaMemcpy(depth, f_depth.data(), sizeof(int) * N, cudaMemcpyHostToDevice));
     GH_CUDA(cudaMemcpy(hld, f_hld.data(), sizeof(int) * N, cudaMemcpyHostToDevice));
+    mark("allocations and uploads");
     {
       const size_t ksmem = (size_t)(max_m + 1) * sizeof(int);
       const int kdyn = enable_max_dynamic_smem(build_positions_kernel);
@@ -592,13 +604,16 @@ FillPlan::FillPlan(const std::vector<Graph *> &graphs, const TilePolicy &pol, co
       GH_CUDA(cudaMemcpy(&e, err, sizeof(int), cudaMemcpyDeviceToHost));
       GH_CHECK(e == 0, H2H_ERR_STATE, "an upper neighbour is not an ancestor in the tree");
     }
+    mark("position lists");
     GH_CUDA(cudaMemcpy(seg_off, f_seg_off.data(), sizeof(int64_t) * (N + 1), cudaMemcpyHostToDevice));
     GH_CUDA(cudaMemcpy(htop, f_htop.data(), sizeof(int) * N, cudaMemcpyHostToDevice));
     GH_CUDA(cudaMemcpy(hpos, f_hpos.data(), sizeof(int) * N, cudaMemcpyHostToDevice));
     root_path_segments_kernel<<<std::max(1, std::min(8192, (N + 255) / 256)), 256>>>(father, depth, htop, hpos,
                                                                                      seg_off, seg_top, seg_pos, N);
     GH_CUDA(cudaGetLastError());
+    mark("root-path segments");
     build_tiles(pol);
+    mark("tiles");
   } catch (...) {
     release_work();
     throw;
@@ -627,13 +642,13 @@ std::vector<int> FillPlan::level_classes() const {
       }
     }
   // narrow: fewer nodes than SMs, whatever their work (the critical path);
-  // heavy: a wider level with at least 2^17 min-plus updates per SM
-  // (GPUH2H_HEAVY_LEVEL_WORK overrides the per-SM figure)
-  int64_t per_sm = int64_t(1) << 17;
-  if (const char *e = std::getenv("GPUH2H_HEAVY_LEVEL_WORK")) per_sm = std::max(1LL, std::atoll(e));
+  // heavy: a wider level whose nodes average at least 2^18 min-plus updates
+  // (GPUH2H_HEAVY_LEVEL_WORK overrides the figure)
+  int64_t per_node = int64_t(1) << 18;
+  if (const char *e = std::getenv("GPUH2H_HEAVY_LEVEL_WORK")) per_node = std::max(1LL, std::atoll(e));
   std::vector<int> cls(nlev, 0);
   for (int l = 0; l < nlev; l++)
-    cls[l] = width[l] < nsm ? 0 : work[l] >= (int64_t)nsm * per_sm ? 2 : 1;
+    cls[l] = width[l] < nsm ? 0 : work[l] >= per_node * width[l] ? 2 : 1;
   return cls;
 }
 
@@ -643,11 +658,20 @@ std::vector<int> FillPlan::level_classes() const {
 // counts per (level, graph), then each graph writes its tiles at the
 // offsets the counts give.
 void FillPlan::build_tiles(const TilePolicy &pol) {
+  const bool trace = std::getenv("GPUH2H_TRACE") != nullptr;
+  Clock tclk;
+  auto mark = [&](const char *what) {
+    if (!trace) return;
+    cudaDeviceSynchronize();
+    std::fprintf(stderr, "[gpuh2h] tiles: %s %.3f ms\n", what, tclk.us() / 1e3);
+    tclk.reset();
+  };
   policy = pol;
   const int K = (int)gs.size();
   int nlev = 0;
   for (const Graph *g : gs) nlev = std::max(nlev, (int)g->tree_hash.size() - 1);
   const std::vector<int> lcls = level_classes();
+  mark("level classes");
   auto tiles_of = [&](int wb, int m, int d, int &nt_node, int &cb, int &sc) {
     const int sb = TilePolicy::sep_bucket(m);
     if ((int64_t)m * d <= pol.small_work[wb][sb]) {
@@ -699,6 +723,7 @@ void FillPlan::build_tiles(const TilePolicy &pol) {
   GH_CHECK(ntiles < INT32_MAX, H2H_ERR_ARG, "too many fill tiles");
   max_u = *std::max_element(mu.begin(), mu.end());
   max_c = *std::max_element(mc.begin(), mc.end());
+  mark("pass 1");
   // pass 2: per node its first ticket, tile count and tile shape; the
   // ticket -> node array is expanded on the device
   std::vector<int> host((size_t)4 * N);
@@ -733,35 +758,47 @@ void FillPlan::build_tiles(const TilePolicy &pol) {
     tiles = dalloc<int>(need, work_bytes);
     tiles_cap = need;
   }
+  mark("pass 2 and allocation");
   // chunks: forest levels in ticket order.  A level with many times more
   // tiles than resident warps hands them out in groups (fewer atomics on the
   // counter); any other level one by one, so its tiles spread over warps.
+  // When every level goes one by one there is no table (chunk k = tile k).
   std::vector<int> chunks;
-  chunks.reserve((size_t)(ntiles / 2 + 1024));
   {
     const int64_t warps = (int64_t)nsm * 64;
-    int64_t t = 0;
+    std::vector<int64_t> lt(nlev, 0);
+    std::vector<int> step(nlev, 1);
+    int64_t nc = 0;
+    bool grouped = false;
     for (int l = 0; l < nlev; l++) {
-      int64_t lt = 0;
       for (int i = 0; i < K; i++)
-        if (l < (int)cnt[i].size()) lt += cnt[i][l];
-      const int step = (int)std::max<int64_t>(1, std::min<int64_t>(8, lt / (8 * warps)));
-      const int64_t e = t + lt;  // this level's tickets are [t, e)
-      for (int64_t c = t; c < e; c += step) chunks.push_back((int)c);
-      t = e;
+        if (l < (int)cnt[i].size()) lt[l] += cnt[i][l];
+      step[l] = (int)std::max<int64_t>(1, std::min<int64_t>(8, lt[l] / (8 * warps)));
+      grouped |= step[l] > 1;
+      nc += (lt[l] + step[l] - 1) / step[l];
     }
-    GH_CHECK(t == ntiles, H2H_ERR_STATE, "fill chunks do not cover the tiles");
-    chunks.push_back((int)ntiles);
+    nchunks = grouped ? nc : ntiles;
+    if (grouped) {
+      chunks.resize((size_t)nc + 1);
+      int64_t t = 0, k = 0;
+      for (int l = 0; l < nlev; l++) {
+        const int64_t e = t + lt[l];  // this level's tickets are [t, e)
+        for (int64_t c = t; c < e; c += step[l]) chunks[k++] = (int)c;
+        t = e;
+      }
+      GH_CHECK(t == ntiles && k == nc, H2H_ERR_STATE, "fill chunks do not cover the tiles");
+      chunks[nc] = (int)ntiles;
+    }
   }
-  for (size_t c = 1; c < chunks.size(); c++)
-    GH_CHECK(chunks[c - 1] < chunks[c], H2H_ERR_STATE, "fill chunk table out of order");
-  nchunks = (int64_t)chunks.size() - 1;
+  mark("chunks");
   GH_CUDA(cudaMemcpy(tiles + ntiles, host.data(), sizeof(int) * 4 * (int64_t)N, cudaMemcpyHostToDevice));
-  GH_CUDA(cudaMemcpy(tiles + ntiles + 4 * (int64_t)N, chunks.data(), sizeof(int) * chunks.size(),
-                     cudaMemcpyHostToDevice));
+  if (!chunks.empty())
+    GH_CUDA(cudaMemcpy(tiles + ntiles + 4 * (int64_t)N, chunks.data(), sizeof(int) * chunks.size(),
+                       cudaMemcpyHostToDevice));
   expand_tiles_kernel<<<std::max(1, std::min(8192, (N * 32 + 255) / 256)), 256>>>(tiles + ntiles, tiles + ntiles + N,
                                                                                   tiles, N);
   GH_CUDA(cudaGetLastError());
+  mark("uploads and expansion");
   const int smem_dyn = enable_max_dynamic_smem(fill_flow_kernel);
   // one staging slice per warp (4 warps per 128-thread block)
   smem = 4 * ((size_t)((max_u + 1) & ~1) * 16 + (size_t)((std::max(max_segs, 1) + 1) & ~1) * 8);
@@ -789,7 +826,7 @@ void FillPlan::enqueue(cudaStream_t s, cudaEvent_t *fill_ev) {
   A.node_ntiles = tiles + ntiles + N;
   A.node_cb = tiles + ntiles + 2 * (int64_t)N;
   A.node_sc = tiles + ntiles + 3 * (int64_t)N;
-  A.chunk_start = tiles + ntiles + 4 * (int64_t)N;
+  A.chunk_start = nchunks == ntiles ? nullptr : tiles + ntiles + 4 * (int64_t)N;
   A.nchunks = (int)nchunks;
   A.node_cnt = done + N;
   A.father = father;

@@ -193,7 +193,7 @@ int h2h_batch_rebuild(h2h_batch *b);
 int h2h_batch_sync_host(h2h_batch *b);
 /* Tile shapes of the forest label fill.  policy is 12 entries
  * "small_work/col_block/sep_chunk" separated by spaces: level class (fewer
- * nodes than SMs / wider / heavy: at least 2^17 min-plus updates per SM),
+ * nodes than SMs / wider / heavy: nodes averaging 2^18+ min-plus updates),
  * times separator size m <= 16, <= 64, <= 256, > 256.
  * h2h_batch_tune times candidate shapes on this batch (coordinate descent,
  * `rounds` passes), keeps the fastest and writes it to policy_out. */
