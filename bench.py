@@ -109,6 +109,15 @@ def batched_build(threads: int, count: int) -> dict:
     tune_s = time.perf_counter() - t0
     reb_tuned = rebuilds()
     check()
+    # label construction alone: one forest fill against the per-graph fills
+    # (our dataflow fill, and the reference's level-by-level mapping)
+    plain_ms, plain_bad = 0.0, 0
+    for gs in seq:
+        ms, bad = gs.fill_labels_plain()
+        plain_ms += ms
+        plain_bad += bad
+    assert plain_bad == 0, "the plain fill mapping disagrees with the labels"
+    single_fill_ms = sum(gs.info()["t_fill_gpu_us"] for gs in seq) / 1e3
     nv = sum(gs.info()["n"] for gs in seq)
     out = {"graphs": count, "vertices": nv, "label_entries": sum(gs.info()["label_size"] for gs in seq),
            "sequential_s": seq_s, "batched_s": batch_s, "speedup_cold": seq_s / batch_s,
@@ -117,6 +126,12 @@ def batched_build(threads: int, count: int) -> dict:
            "elim_launches": cold["elim_launches"], "fill_tiles": cold["fill_tiles"],
            "rebuild_s_default_tiles": reb_default, "rebuild_s_tuned_tiles": reb_tuned,
            "speedup_rebuild_vs_sequential": seq_s / reb_tuned, "tuned_policy": policy, "tune_s": tune_s,
+           "label_construction": {
+               "batched_fill_ms": cold["t_fill_us"] / 1e3, "sequential_dataflow_fills_ms": single_fill_ms,
+               "sequential_plain_fills_ms": plain_ms,
+               "speedup_vs_plain": plain_ms / (cold["t_fill_us"] / 1e3),
+               "speedup_vs_sequential_dataflow": single_fill_ms / (cold["t_fill_us"] / 1e3),
+               "plain": "the reference's mapping: one thread per (v,u) pair, one launch + sync per tree level"},
            "parity": "answers to 1e4 pairs per graph, max label and label count equal the sequential builds'"}
     b.close()
     for g in seq + bat:
@@ -576,7 +591,11 @@ def main():
     # L4 fill: own rows read+written, separator lists, one ancestor entry per update
     fill_s = info["t_fill_gpu_us"] / 1e6
     fill_bytes = 8 * info["label_size"] + 8 * info["pos_size"] + 4 * info["label_updates"]
+    plain_fill_ms, plain_fill_bad = g.fill_labels_plain()
+    assert plain_fill_bad == 0, "the plain fill mapping disagrees with the labels"
     fill = {"kernel": "fill_flow_kernel", "updates": info["label_updates"], "seconds": fill_s,
+            "plain_gpu_seconds": plain_fill_ms / 1e3,
+            "plain_gpu": "the reference's mapping: one thread per (v,u) pair, one launch + sync per tree level",
             "updates_per_s": info["label_updates"] / fill_s if fill_s > 0 else None,
             "algorithmic_bytes": fill_bytes,
             "achieved_gbs": fill_bytes / fill_s / 1e9 if fill_s > 0 else None,

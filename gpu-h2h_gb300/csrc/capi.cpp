@@ -192,6 +192,11 @@ int h2h_query_batch_plain(const h2h_graph *h, const int *x_dev, const int *y_dev
   });
 }
 
+int h2h_fill_labels_plain(const h2h_graph *h, double *ms, int64_t *mismatches) {
+  if (!h) { gh::set_last_error("null handle"); return H2H_ERR_ARG; }
+  return guarded([&] { gh::fill_labels_plain(h->g, ms, mismatches); });
+}
+
 int h2h_query_batch_host(const h2h_graph *hc, const int *x, const int *y, int *out, int64_t n, int mode) {
   if (!hc) { gh::set_last_error("null handle"); return H2H_ERR_ARG; }
   h2h_graph *h = const_cast<h2h_graph *>(hc);

@@ -351,6 +351,36 @@ __global__ void __launch_bounds__(128) fill_flow_kernel(FlowArgs A) {
   }
 }
 
+// The reference's GPU label fill mapping, kept as a measurement baseline
+// (makeH2HLabel_noCommunication_D_noHub_3, kernel_functions.cu:717-744, with
+// the L4 block :738-743 enabled): one thread per (v, u) pair of one tree
+// level; the thread min-updates the columns above u directly and walks
+// father pointers for the columns below u.  Launched once per level with a
+// device synchronisation in between, as the reference does.
+__global__ void plain_fill_level_kernel(const int *pair_v, const int64_t *pair_k, int npairs, const int64_t *drow,
+                                        const int *depth, const int *father, const int *pos_pos, const int *pos_id,
+                                        const int *pos_w, int *dis) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < npairs; i += gridDim.x * blockDim.x) {
+    const int v = pair_v[i];
+    const int64_t k = pair_k[i];
+    const int p = pos_pos[k], u = pos_id[k], t = pos_w[k], d = depth[v];
+    const int64_t base = drow[v], ub = drow[u];
+    for (int j = 0; j < p; j++) atomicMin(dis + base + j, t + __ldcg(dis + ub + j));
+    int a = father[v];
+    for (int j = d - 2; j > p && a >= 0; j--) {
+      atomicMin(dis + base + j, t + __ldcg(dis + drow[a] + p));
+      a = father[a];
+    }
+  }
+}
+
+__global__ void count_mismatch_kernel(const int *a, const int *b, int64_t n, unsigned long long *bad) {
+  unsigned long long c = 0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    c += a[i] != b[i];
+  if (c) atomicAdd(bad, c);
+}
+
 // tile_node[t] = v for the tickets of every node v.  One warp per node.
 __global__ void expand_tiles_kernel(const int *node_first, const int *node_ntiles, int *tile_node, int n) {
   const int lane = threadIdx.x & 31;
@@ -1169,6 +1199,121 @@ void upload_labels(Graph &g, const std::vector<int> &dis, const std::vector<int>
   }
   cudaFreeHost(stage);
   g.drow_host.swap(drow);
+}
+
+// Runs the reference's mapping (plain_fill_level_kernel) on the built graph
+// into a scratch copy of the rows and compares it with the built labels.
+// The device time of the per-level launches and synchronisations goes to
+// *ms; *mismatches receives the number of differing entries.
+void fill_labels_plain(const Graph &g, double *ms, int64_t *mismatches) {
+  GH_CHECK(g.labelled && g.label_mode == H2H_LABEL_L4, H2H_ERR_STATE, "needs built L4 labels");
+  const DeviceIndex &D = g.dev;
+  const int n = g.n;
+  const int64_t np = g.pos_hash[n];
+  std::vector<int> pid(np), ppos(np);
+  download_positions(g, pid.data(), ppos.data());
+  // (v, k) pairs per tree level, k over v's entries other than v itself
+  std::vector<int> pv;
+  std::vector<int64_t> pk;
+  std::vector<int64_t> lvl_off{0};
+  const int nlev = (int)g.tree_hash.size() - 1;
+  for (int l = 0; l < nlev; l++) {
+    for (int q = g.tree_hash[l]; q < g.tree_hash[l + 1]; q++) {
+      const int v = g.tree_bfs[q];
+      for (int64_t k = g.pos_hash[v]; k < g.pos_hash[v + 1]; k++)
+        if (pid[k] != v) { pv.push_back(v); pk.push_back(k); }
+    }
+    lvl_off.push_back((int64_t)pv.size());
+  }
+  int64_t tmp = 0;
+  int *d_dis = nullptr, *d_pv = nullptr, *d_w = nullptr;
+  int64_t *d_pk = nullptr, *d_drow = nullptr;
+  int *d_depth = nullptr, *d_father = nullptr, *d_pos_pos = nullptr, *d_pos_id = nullptr;
+  int64_t *d_pos_hash = nullptr;
+  unsigned long long *d_bad = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  auto cleanup = [&]() {
+    cudaFree(d_dis); cudaFree(d_pv); cudaFree(d_w); cudaFree(d_pk); cudaFree(d_drow); cudaFree(d_depth);
+    cudaFree(d_father); cudaFree(d_pos_pos); cudaFree(d_pos_id); cudaFree(d_pos_hash); cudaFree(d_bad);
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+  };
+  try {
+    const int64_t rows = g.drow_host[n] - g.drow_host[0];
+    std::vector<int64_t> drow(n + 1);
+    for (int v = 0; v <= n; v++) drow[v] = g.drow_host[v] - g.drow_host[0];
+    std::vector<int> pw(np);
+    {
+      // shortcut weights per position entry from the device lists
+      std::vector<int> xid(g.x_off[n]), xw(g.x_off[n]);
+      if (g.x_off[n]) {
+        GH_CUDA(cudaMemcpy(xid.data(), D.lists.id + D.x_base, sizeof(int) * g.x_off[n], cudaMemcpyDeviceToHost));
+        GH_CUDA(cudaMemcpy(xw.data(), D.lists.w + D.x_base, sizeof(int) * g.x_off[n], cudaMemcpyDeviceToHost));
+      }
+      for (int v = 0; v < n; v++)  // lists are sorted by id: binary search
+        for (int64_t k = g.pos_hash[v]; k < g.pos_hash[v + 1]; k++) {
+          pw[k] = 0;
+          if (pid[k] == v) continue;
+          const auto b = xid.begin() + g.x_off[v], e = xid.begin() + g.x_off[v + 1];
+          const auto it = std::lower_bound(b, e, pid[k] + D.id_base);
+          if (it != e && *it == pid[k] + D.id_base) pw[k] = xw[it - xid.begin()];
+        }
+    }
+    d_dis = dalloc<int>(rows, tmp);
+    d_pv = dalloc<int>(std::max<size_t>(pv.size(), 1), tmp);
+    d_pk = dalloc<int64_t>(std::max<size_t>(pk.size(), 1), tmp);
+    d_drow = dalloc<int64_t>(n + 1, tmp);
+    d_depth = dalloc<int>(n, tmp);
+    d_father = dalloc<int>(n, tmp);
+    d_pos_pos = dalloc<int>(std::max<int64_t>(np, 1), tmp);
+    d_pos_id = dalloc<int>(std::max<int64_t>(np, 1), tmp);
+    d_w = dalloc<int>(std::max<int64_t>(np, 1), tmp);
+    d_pos_hash = dalloc<int64_t>(n + 1, tmp);
+    d_bad = dalloc<unsigned long long>(1, tmp);
+    if (!pv.empty()) {
+      GH_CUDA(cudaMemcpy(d_pv, pv.data(), sizeof(int) * pv.size(), cudaMemcpyHostToDevice));
+      GH_CUDA(cudaMemcpy(d_pk, pk.data(), sizeof(int64_t) * pk.size(), cudaMemcpyHostToDevice));
+    }
+    GH_CUDA(cudaMemcpy(d_drow, drow.data(), sizeof(int64_t) * (n + 1), cudaMemcpyHostToDevice));
+    GH_CUDA(cudaMemcpy(d_depth, g.depth.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
+    GH_CUDA(cudaMemcpy(d_father, g.father.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
+    GH_CUDA(cudaMemcpy(d_pos_pos, ppos.data(), sizeof(int) * np, cudaMemcpyHostToDevice));
+    GH_CUDA(cudaMemcpy(d_pos_id, pid.data(), sizeof(int) * np, cudaMemcpyHostToDevice));
+    GH_CUDA(cudaMemcpy(d_w, pw.data(), sizeof(int) * np, cudaMemcpyHostToDevice));
+    GH_CUDA(cudaMemcpy(d_pos_hash, g.pos_hash.data(), sizeof(int64_t) * (n + 1), cudaMemcpyHostToDevice));
+    GH_CUDA(cudaMemset(d_bad, 0, sizeof(unsigned long long)));
+    GH_CUDA(cudaEventCreate(&e0));
+    GH_CUDA(cudaEventCreate(&e1));
+    GH_CUDA(cudaEventRecord(e0));
+    // mallocH2HLabel_noHub's initial rows, then the levels in order
+    init_rows_kernel<<<std::max(1, std::min(65535, (n * 32 + 255) / 256)), 256>>>(d_drow, d_depth, d_pos_hash,
+                                                                                  d_pos_pos, d_w, d_dis, n);
+    GH_CUDA(cudaGetLastError());
+    GH_CUDA(cudaDeviceSynchronize());
+    for (int l = 1; l < nlev; l++) {
+      const int64_t a = lvl_off[l], b = lvl_off[l + 1];
+      if (b == a) continue;
+      const int cnt = (int)(b - a);
+      plain_fill_level_kernel<<<(cnt + 255) / 256, 256>>>(d_pv + a, d_pk + a, cnt, d_drow, d_depth, d_father,
+                                                           d_pos_pos, d_pos_id, d_w, d_dis);
+      GH_CUDA(cudaGetLastError());
+      GH_CUDA(cudaDeviceSynchronize());
+    }
+    GH_CUDA(cudaEventRecord(e1));
+    GH_CUDA(cudaEventSynchronize(e1));
+    float t = 0;
+    GH_CUDA(cudaEventElapsedTime(&t, e0, e1));
+    if (ms) *ms = t;
+    count_mismatch_kernel<<<1024, 256>>>(d_dis, D.dis + g.drow_host[0], rows, d_bad);
+    GH_CUDA(cudaGetLastError());
+    unsigned long long bad = 0;
+    GH_CUDA(cudaMemcpy(&bad, d_bad, sizeof(bad), cudaMemcpyDeviceToHost));
+    if (mismatches) *mismatches = (int64_t)bad;
+  } catch (...) {
+    cleanup();
+    throw;
+  }
+  cleanup();
 }
 
 // Position lists in the reference layout with graph-local ids: the host

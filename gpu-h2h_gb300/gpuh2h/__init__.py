@@ -109,6 +109,7 @@ SIGNATURES = {
                                           _vp]),
     "h2h_copy_input_arcs": (_i32, [_vp, _vp, _vp, _vp]),
     "h2h_save_index": (_i32, [_vp, _cp]),
+    "h2h_fill_labels_plain": (_i32, [_vp, C.POINTER(C.c_double), C.POINTER(_i64)]),
     "h2h_load_index": (_i32, [_cp, C.POINTER(_vp)]),
     "h2h_batch_build": (_i32, [_vp, _i32, _i32, C.POINTER(_vp)]),
     "h2h_batch_set_weights": (_i32, [_vp, _i32, _vp]),
@@ -214,6 +215,14 @@ class Graph:
         g.h = h
         g.graphName = graphName
         return g
+
+    def fill_labels_plain(self):
+        """(device ms, mismatching entries) of the reference's fill mapping
+        re-run on this graph (measurement baseline)."""
+        ms = C.c_double()
+        bad = C.c_int64()
+        _check(self._L.h2h_fill_labels_plain(self.h, C.byref(ms), C.byref(bad)))
+        return ms.value, bad.value
 
     def save_index(self, path: str):
         _check(self._L.h2h_save_index(self.h, path.encode()))

@@ -55,6 +55,15 @@ int h2h_gen_local_pairs(const h2h_graph *g, int64_t n, int max_hops, uint64_t se
 int h2h_query_batch_plain(const h2h_graph *g, const int *x_dev, const int *y_dev, int *out_dev, int64_t n,
                           int mode, void *stream);
 
+/* Measurement baseline, not a product path: the labels of a built L4 graph
+ * recomputed with the reference's GPU fill mapping (one thread per (v, u)
+ * pair, one launch and one device synchronisation per tree level, father-
+ * pointer walks for the L4 columns; kernel_functions.cu:717-744,
+ * tanslate.cu:511-617) into scratch rows.  *ms receives the device time,
+ * *mismatches the entries that differ from the built labels (0 expected:
+ * L4 labels are exact whatever the order). */
+int h2h_fill_labels_plain(const h2h_graph *g, double *ms, int64_t *mismatches);
+
 /* Load generator for a query server (measurement tool).  Each request goes
  * to a uniformly drawn graph of graph_ids (vertex counts graph_n) with a
  * size drawn log-uniform in [size_lo, size_hi] pairs of uniform vertices.

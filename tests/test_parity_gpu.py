@@ -188,3 +188,13 @@ def test_tile_policies(cfg0_root, golden0, monkeypatch, policy):
     monkeypatch.setenv("GPUH2H_TILE_POLICY", policy)
     g = build(gpuh2h.files_for(cfg0_root, "cfg0"), 6, 2)
     assert np.array_equal(_sha(g.labels()["dis"]), golden0["cfg0_C2_L4/sha256/dis"])
+
+
+def test_plain_fill_baseline_matches(cfg0_root):
+    """The reference's level-by-level fill mapping (the measurement baseline)
+    reproduces the dataflow fill's labels exactly."""
+    import gpuh2h
+    for C in (1, 2):
+        g = build(gpuh2h.files_for(cfg0_root, "cfg0"), 6, C)
+        ms, bad = g.fill_labels_plain()
+        assert bad == 0 and ms > 0
