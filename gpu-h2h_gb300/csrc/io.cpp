@@ -12,6 +12,7 @@
 
 #include "graph.h"
 #include "gpuh2h_tools.h"
+#include "pool.h"
 
 namespace gh {
 
@@ -63,6 +64,85 @@ struct Cursor {
   }
 };
 
+// The arcs of an Edge file in parallel, for files with one arc per line:
+// the text after the header is cut into chunks at line starts, each chunk is
+// parsed on its own (marker, u, v, w per arc) and must end on an arc
+// boundary; the first m arcs are kept in file order, self loops dropped.
+// Returns false (nothing kept) when the file needs the token-by-token reader:
+// an arc spread over lines, fewer than m arcs, anything unparsable.  Ids and
+// weights out of range still raise H2H_ERR_FORMAT.
+bool parse_arcs_parallel(const Cursor &c0, long long m, int n, int threads, std::vector<int> &eu,
+                         std::vector<int> &ev, std::vector<int> &ew) {
+  const char *b = c0.p, *e = c0.e;
+  if (m == 0 || threads < 2 || e - b < (1 << 20)) return false;
+  const int T = threads;
+  std::vector<const char *> cut(T + 1, e);
+  cut[0] = b;
+  for (int t = 1; t < T; t++) {
+    const char *q = b + (e - b) * t / T;
+    while (q < e && *q != '\n') q++;
+    cut[t] = q < e ? q + 1 : e;
+  }
+  struct Part {
+    std::vector<int> u, v, w;
+    bool ok = true, range = true;
+  };
+  std::vector<Part> parts(T);
+  Pool pool(T);
+  pool.parallel_for(T, 1, [&](int64_t lo, int64_t hi, int) {
+    for (int64_t t = lo; t < hi; t++) {
+      Part &P = parts[t];
+      static const std::string kEmpty;
+      Cursor c(kEmpty, c0.what);
+      c.p = cut[t];
+      c.e = cut[t + 1];
+      try {
+        for (;;) {
+          c.skip();
+          if (c.p >= c.e) break;
+          c.one_char();
+          const long long a = c.integer(), bb = c.integer(), w = c.integer();
+          if (a < 1 || a > n || bb < 1 || bb > n || w < 0 || w > INT32_MAX) { P.range = false; break; }
+          P.u.push_back((int)a - 1);
+          P.v.push_back((int)bb - 1);
+          P.w.push_back((int)w);
+          // an arc must end its line: the next non-blank character is on a new line
+          const char *q = c.p;
+          while (q < c.e && (*q == ' ' || *q == '\t' || *q == '\r')) q++;
+          if (q < c.e && *q != '\n') { P.ok = false; break; }
+        }
+      } catch (const Error &) {
+        P.ok = false;
+      }
+    }
+  });
+  long long total = 0;
+  for (int t = 0; t < T; t++) {
+    if (!parts[t].ok) return false;
+    if (!parts[t].range) {
+      // only an error if the bad arc is among the first m
+      if (total + (long long)parts[t].u.size() < m)
+        throw Error(H2H_ERR_FORMAT, "vertex id or weight out of range in " + c0.what);
+      break;
+    }
+    total += (long long)parts[t].u.size();
+    if (total >= m) break;
+  }
+  if (total < m) return false;
+  eu.reserve(m);
+  ev.reserve(m);
+  ew.reserve(m);
+  long long taken = 0;
+  for (int t = 0; t < T && taken < m; t++)
+    for (size_t i = 0; i < parts[t].u.size() && taken < m; i++, taken++) {
+      if (parts[t].u[i] == parts[t].v[i]) continue;  // self loops dropped
+      eu.push_back(parts[t].u[i]);
+      ev.push_back(parts[t].v[i]);
+      ew.push_back(parts[t].w[i]);
+    }
+  return true;
+}
+
 }  // namespace
 
 // Graph_D_H::Graph::Graph (Graph_Fundamental.cu:4-95).  Inputs that the
@@ -97,17 +177,21 @@ void load_graph(Graph &g, const std::string &edge, const std::string &idf, const
     GH_CHECK(n2 == g.n, H2H_ERR_FORMAT, "vertex count of " + edge + " differs from " + idf);
     GH_CHECK(m >= 0 && m < (1LL << 40), H2H_ERR_FORMAT, "bad arc count in " + edge);
     std::vector<int> eu, ev, ew;
-    eu.reserve(m); ev.reserve(m); ew.reserve(m);
-    std::vector<int> cnt(g.n + 1, 0);
-    for (long long i = 0; i < m; i++) {                   // :46-55
-      c.one_char();
-      long long a = c.integer(), b = c.integer(), w = c.integer();
-      GH_CHECK(a >= 1 && a <= g.n && b >= 1 && b <= g.n, H2H_ERR_FORMAT, "vertex id out of range in " + edge);
-      GH_CHECK(w >= 0 && w <= INT32_MAX, H2H_ERR_FORMAT, "weight out of range in " + edge);
-      if (a == b) continue;                               // self loops dropped
-      eu.push_back((int)a - 1); ev.push_back((int)b - 1); ew.push_back((int)w);
-      cnt[a - 1]++;
+    if (!parse_arcs_parallel(c, m, g.n, std::max(1, g.threads), eu, ev, ew)) {
+      // the reference's stream semantics, one token at a time
+      eu.clear(); ev.clear(); ew.clear();
+      eu.reserve(m); ev.reserve(m); ew.reserve(m);
+      for (long long i = 0; i < m; i++) {                 // :46-55
+        c.one_char();
+        long long a = c.integer(), b = c.integer(), w = c.integer();
+        GH_CHECK(a >= 1 && a <= g.n && b >= 1 && b <= g.n, H2H_ERR_FORMAT, "vertex id out of range in " + edge);
+        GH_CHECK(w >= 0 && w <= INT32_MAX, H2H_ERR_FORMAT, "weight out of range in " + edge);
+        if (a == b) continue;                             // self loops dropped
+        eu.push_back((int)a - 1); ev.push_back((int)b - 1); ew.push_back((int)w);
+      }
     }
+    std::vector<int> cnt(g.n + 1, 0);
+    for (int a : eu) cnt[a]++;
     g.m = (int64_t)eu.size();
     g.adj_off.assign(g.n + 1, 0);
     for (int i = 0; i < g.n; i++) g.adj_off[i + 1] = g.adj_off[i] + cnt[i];
