@@ -742,16 +742,7 @@ GraphLevels graph_levels(const Graph &g) {
     for (int64_t c = lo; c <= hi; c++)
       for (int i = 0; i < g.cell_count[c]; i++) L.level_of[g.elim[g.cell_start[c] + i]] = h;
   }
-  L.dup.assign(n, 0);
-  for (int v = 0; v < n; v++) {
-    const int b = g.adj_off[v], e = g.adj_off[v + 1];
-    bool sorted = true;
-    for (int i = b + 1; i < e && sorted; i++) sorted = g.adj_v[i - 1] < g.adj_v[i];
-    if (sorted) continue;  // strictly increasing: no parallel arcs
-    std::vector<int> tmp(g.adj_v.begin() + b, g.adj_v.begin() + e);
-    std::sort(tmp.begin(), tmp.end());
-    L.dup[v] = (int)(tmp.size() - (std::unique(tmp.begin(), tmp.end()) - tmp.begin()));
-  }
+  L.dup.assign(n, 0);  // filled by count_parallel_arcs
   // global order: the vertices of cells at levels C..1 (tail of elim)
   int64_t heap_start = INT32_MAX;
   for (int h = g.C; h > 0; h--) {
@@ -762,6 +753,21 @@ GraphLevels graph_levels(const Graph &g) {
   L.heap_start = (int)heap_start;
   L.heap_n = n - (int)heap_start;
   return L;
+}
+
+// Parallel-arc count of the vertices [b, e) (duplicate neighbour ids in the
+// input list), into L.dup.
+void count_parallel_arcs(const Graph &g, GraphLevels &L, int b, int e) {
+  std::vector<int> tmp;
+  for (int v = b; v < e; v++) {
+    const int lo = g.adj_off[v], hi = g.adj_off[v + 1];
+    bool sorted = true;
+    for (int i = lo + 1; i < hi && sorted; i++) sorted = g.adj_v[i - 1] < g.adj_v[i];
+    if (sorted) continue;  // strictly increasing: no parallel arcs
+    tmp.assign(g.adj_v.begin() + lo, g.adj_v.begin() + hi);
+    std::sort(tmp.begin(), tmp.end());
+    L.dup[v] = (int)(tmp.size() - (std::unique(tmp.begin(), tmp.end()) - tmp.begin()));
+  }
 }
 
 // Bound on a list of cell c while level h runs: alive cell members - 1 +
@@ -802,18 +808,13 @@ ElimPlan::ElimPlan(const std::vector<Graph *> &graphs) : gs(graphs) {
   int threads = 1;
   for (const Graph *g : gs) threads = std::max(threads, g->threads);
   {
-    Pool pool(std::min(threads, K));
+    Pool pool(threads);
     std::vector<std::exception_ptr> errs(K);
     pool.parallel_for(K, 1, [&](int64_t lo, int64_t hi, int) {
       for (int64_t i = lo; i < hi; i++) {
         try {
-          const Graph &g = *gs[i];
-          L[i] = graph_levels(g);
-          bound[i].assign(g.cell_start.size(), 1);
-          for (int h = g.H; h > g.C; h--) {
-            const int64_t clo = (int64_t(1) << (h - 1)) - 1, chi = (int64_t(1) << h) - 2;
-            for (int64_t c = clo; c <= chi; c++) bound[i][c] = cell_list_bound(g, L[i], c, h);
-          }
+          L[i] = graph_levels(*gs[i]);
+          bound[i].assign(gs[i]->cell_start.size(), 1);
         } catch (...) {
           errs[i] = std::current_exception();
         }
@@ -821,6 +822,33 @@ ElimPlan::ElimPlan(const std::vector<Graph *> &graphs) : gs(graphs) {
     });
     for (auto &e : errs)
       if (e) std::rethrow_exception(e);
+    // parallel-arc counts, vertex chunks of every graph in parallel
+    struct VertexTask {
+      int i, b, e;
+    };
+    std::vector<VertexTask> vtasks;
+    for (int i = 0; i < K; i++)
+      for (int b = 0; b < gs[i]->n; b += 4096) vtasks.push_back({i, b, std::min(gs[i]->n, b + 4096)});
+    pool.parallel_for((int64_t)vtasks.size(), 1, [&](int64_t lo, int64_t hi, int) {
+      for (int64_t t = lo; t < hi; t++) count_parallel_arcs(*gs[vtasks[t].i], L[vtasks[t].i], vtasks[t].b, vtasks[t].e);
+    });
+    // list bounds of every partition cell of every graph, cells in parallel
+    struct CellTask {
+      int i, h;
+      int64_t c;
+    };
+    std::vector<CellTask> tasks;
+    for (int i = 0; i < K; i++)
+      for (int h = gs[i]->H; h > gs[i]->C; h--) {
+        const int64_t clo = (int64_t(1) << (h - 1)) - 1, chi = (int64_t(1) << h) - 2;
+        for (int64_t c = clo; c <= chi; c++) tasks.push_back({i, h, c});
+      }
+    pool.parallel_for((int64_t)tasks.size(), 8, [&](int64_t lo, int64_t hi, int) {
+      for (int64_t t = lo; t < hi; t++) {
+        const CellTask &T = tasks[t];
+        bound[T.i][T.c] = cell_list_bound(*gs[T.i], L[T.i], T.c, T.h);
+      }
+    });
   }
   std::vector<int64_t> lbase(K);
   vbase.assign(K, 0);
