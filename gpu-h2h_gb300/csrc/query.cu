@@ -332,12 +332,6 @@ void run_query_batch(const Graph &g, const int *x, const int *y, int *out, int64
   const DeviceIndex &D = g.dev;
   QArgs A{x, y, out, n, g.n, D.first, D.depth, D.rmq_hash, D.rmq_id, D.pos_hash, D.pos_pos, D.drow, D.dis,
           bad ? bad : D.err};
-  static int nsm = 0;
-  if (!nsm) {
-    int dev = 0;
-    GH_CUDA(cudaGetDevice(&dev));
-    GH_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-  }
   const int threads = 256;
   const int mi = mode == H2H_QUERY_LCA ? 0 : 1;
   using Kernel = void (*)(QArgs);
@@ -346,11 +340,24 @@ void run_query_batch(const Graph &g, const int *x, const int *y, int *out, int64
        query_tile_kernel<true, 4>},
       {query_tile_kernel<false, 32>, query_tile_kernel<false, 16>, query_tile_kernel<false, 8>,
        query_tile_kernel<false, 4>}};
-  static int per_sm[2] = {0, 0};  // resident 256-thread blocks per SM (all tile widths use 32 registers)
-  if (!per_sm[mi]) {
-    GH_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm[mi], kernels[mi][0], threads, 0));
-    per_sm[mi] = std::max(1, per_sm[mi]);
-  }
+  // device shape, looked up once (thread-safe static initialisation: the
+  // server's worker and callers' threads may arrive together)
+  struct Shape {
+    int nsm = 1, per_sm[2] = {1, 1};  // resident 256-thread blocks per SM (all tile widths use 32 registers)
+  };
+  static const Shape shape = [] {
+    Shape sh;
+    int dev = 0;
+    GH_CUDA(cudaGetDevice(&dev));
+    GH_CUDA(cudaDeviceGetAttribute(&sh.nsm, cudaDevAttrMultiProcessorCount, dev));
+    for (int k = 0; k < 2; k++) {
+      GH_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&sh.per_sm[k], kernels[k][0], 256, 0));
+      sh.per_sm[k] = std::max(1, sh.per_sm[k]);
+    }
+    return sh;
+  }();
+  const int nsm = shape.nsm;
+  const int per_sm[2] = {shape.per_sm[0], shape.per_sm[1]};
   // narrowest tile whose warps still fit one wave of resident warps
   const int64_t resident_warps = (int64_t)nsm * per_sm[mi] * (threads / 32);
   int ti = 0, tile = 32;
