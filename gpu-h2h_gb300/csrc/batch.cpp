@@ -26,7 +26,7 @@
 #include "pool.h"
 
 namespace gh {
-std::string tile_policy_tune(FillPlan &plan, ElimPlan &elim, cudaStream_t s, int rounds);
+std::string tile_policy_tune(FillPlan &plan, cudaStream_t s, int rounds);
 }
 
 struct h2h_batch {
@@ -277,7 +277,7 @@ int h2h_batch_tune(h2h_batch *b, int rounds, char *policy_out, int cap) {
     GH_CHECK(rounds >= 1 && rounds <= 8, H2H_ERR_ARG, "rounds must be 1..8");
     GH_CUDA(cudaStreamSynchronize(b->stream));
     b->drop_graph();
-    const std::string p = gh::tile_policy_tune(*b->fill, *b->elim, b->stream, rounds);
+    const std::string p = gh::tile_policy_tune(*b->fill, b->stream, rounds);
     b->fill->attach(false);
     b->fill_info();
     copy_policy(p, policy_out, cap);

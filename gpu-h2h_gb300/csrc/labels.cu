@@ -8,14 +8,17 @@
 //   t = dis[v][p]
 //   dis[v][j] = min(dis[v][j], t + dis[u][j])            j < p   (ancestors above u)
 //   dis[v][j] = min(dis[v][j], t + dis[anc_j(v)][p])     p < j < d-1 (L4: below u)
-// Rows of a tree level depend only on rows of shallower levels, so levels run
-// in order and the nodes of a level in parallel: one warp owns a node, keeps
-// its row in shared memory (lanes own columns, no atomics), reads u's row
-// with coalesced loads and the L4 column entries through the ancestor chain.
-// The chain (row offsets of the node's ancestors) is staged in shared memory
-// from the father's chain, which the previous level wrote to a ping-pong
-// buffer.  The update order is the reference's, so L3 rows match its PF CPU
-// fill and L4 rows equal exact ancestor distances.
+//
+// Three fills live here:
+//   * fill_flow_kernel, the L4 fill: a dataflow over tiles of the forest of
+//     one or more graphs, one warp per tile (FillPlan, further down);
+//   * fill_level_kernel, level-synchronous, one warp per node in the
+//     reference's update order: L3 rows (order-dependent) and L4 on request;
+//     the node's row stays in shared memory, and its ancestors' row offsets
+//     are staged from the father's, which the previous level wrote to a
+//     ping-pong buffer;
+//   * plain_fill_level_kernel, the reference's own mapping (one thread per
+//     (v, u) pair, a launch per level), kept as a measurement baseline.
 //
 // Rows are padded to 16-byte starts (drow[v] is a multiple of 4 ints) so the
 // u-row reads are 128-bit vector loads.
@@ -939,7 +942,7 @@ void FillPlan::attach(bool first) {
 // split, each candidate timed as a whole fill (best of two runs) with the
 // other buckets held; a candidate replaces the incumbent only when it is 2%
 // faster.  Any policy gives the same labels: only the schedule changes.
-std::string tile_policy_tune(FillPlan &plan, ElimPlan &elim, cudaStream_t s, int rounds) {
+std::string tile_policy_tune(FillPlan &plan, cudaStream_t s, int rounds) {
   bool used[TilePolicy::kWidth][TilePolicy::kSep] = {};
   {
     const std::vector<int> lcls = plan.level_classes();
