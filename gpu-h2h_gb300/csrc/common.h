@@ -4,8 +4,10 @@
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <chrono>
 #include <cstdint>
+#include <cstdlib>
 #include <cstdio>
 #include <stdexcept>
 #include <string>
@@ -58,6 +60,15 @@ inline int enable_max_dynamic_smem(K kernel) {
   int dyn = optin - (int)fa.sharedSizeBytes;
   GH_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
   return dyn;
+}
+
+// Bound on one spin-wait of a kernel (a dependency or a barrier), in SM clock
+// cycles: 2 s at 2 GHz, or GPUH2H_SPIN_LIMIT_MS (profilers replay
+// instrumented kernels much slower).
+inline long long spin_limit_cycles() {
+  long long ms = 2000;
+  if (const char *e = std::getenv("GPUH2H_SPIN_LIMIT_MS")) ms = std::max(1LL, std::atoll(e));
+  return ms * 2000000LL;
 }
 
 inline int ilog2_floor(int64_t x) {  // floor(log2(x)) for x >= 1; equals (int)log2((double)x)

@@ -49,6 +49,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <exception>
+#include <queue>
 
 #include "graph.h"
 #include "pool.h"
@@ -62,6 +63,8 @@ namespace {
 constexpr int kErrOverflow = 1;  // a list outgrew its LUB capacity (the reference corrupts memory)
 constexpr int kErrEmpty = 2;     // eliminated a vertex without neighbours (the reference reads out of bounds)
 constexpr int kErrStaging = 3;   // a list outgrew the per-level staging bound
+constexpr int kErrTimeout = 4;   // a cell barrier wait ran out (cell_grid_kernel)
+constexpr int kErrPick = 5;      // no candidate left to pick (inconsistent cell table)
 
 struct ElimArgs {
   int *slot_nbr;
@@ -113,17 +116,44 @@ __device__ __forceinline__ int corank(const int *pid, int np, const int *aid, in
   return lo;
 }
 
+// What a merge needs to know about neighbour u: list start, length (junk
+// prefix included), junk prefix, and -- loaded up front in the same round
+// trip when kPre, else where they are used -- capacity, height, candidate
+// index.  Only the warp merging u writes these during an elimination (the
+// candidate index changes only when u is picked).  kPre costs registers: the
+// cluster kernel, which wants several CTAs per SM, loads late.
+struct NbrMeta {
+  int64_t off;
+  int s, J, cap, h, p;
+};
+
+// Mutable global data is read through L2 (ld.global.cg): other CTAs write it
+// between barriers.
+template <bool kPre>
+__device__ __forceinline__ NbrMeta load_meta(const ElimArgs &A, int u) {
+  NbrMeta m;
+  m.off = __ldcg(A.slot_off + u);
+  m.s = __ldcg(A.lsize + u);
+  m.J = __ldcg(A.ljunk + u);
+  if (kPre) {
+    m.cap = __ldcg(A.cap + u);
+    m.h = __ldcg(A.height + u);
+    m.p = __ldcg(A.cpos + u);
+  }
+  return m;
+}
+
 // Rebuild neighbour u's list for the elimination of v (one warp):
 //   P = valid entries of u's list except v (kernel_functions.cu:364-390),
 //   output = P with the first entry of every matched id min-updated, plus the
 //   unmatched members of Q inserted in order (:392-457).
-// Mutable global data is read through L2 (ld.global.cg): other CTAs of the
-// cluster write it between cluster barriers.
-__device__ void merge_neighbour(const ElimArgs &A, int u, int wu, int iu, int v, int hnow, const int *aid,
-                                const int *aw, int c, int *pid, int *pw, int lane, Cand cand) {
-  int64_t off = __ldcg(A.slot_off + u);
-  const int s = __ldcg(A.lsize + u);
-  const int J = __ldcg(A.ljunk + u);
+template <bool kPre>
+__device__ void merge_neighbour(const ElimArgs &A, int u, const NbrMeta &m, int wu, int iu, int v, int hnow,
+                                const int *aid, const int *aw, int c, int *pid, int *pw, int lane, Cand cand,
+                                int nslots) {
+  int64_t off = m.off;
+  const int s = m.s;
+  const int J = m.J;
   int np = 0;
   // u's list minus v, loaded four warp-widths at a time so the L2 round trips overlap
   for (int base = J; base < s; base += 128) {
@@ -183,12 +213,13 @@ __device__ void merge_neighbour(const ElimArgs &A, int u, int wu, int iu, int v,
     if (lane >= o) incl += y;
   }
   const int total = __shfl_sync(0xffffffffu, incl, 31);
-  bool fits = Jn + total <= __ldcg(A.cap + u);
+  const int capu = kPre ? m.cap : __ldcg(A.cap + u);
+  bool fits = Jn + total <= capu;
   if (!fits && A.heap_mode) {
     // the reference's heap adjacency is a hash map that grows freely: move the
     // list to a fresh range (the merge writes a full new copy anyway)
     int64_t fresh = -1;
-    const int ncap = max(2 * __ldcg(A.cap + u), Jn + total);
+    const int ncap = max(2 * capu, Jn + total);
     if (lane == 0) {
       const unsigned long long at = atomicAdd(A.pool_next, (unsigned long long)ncap);
       if ((int64_t)at + ncap <= A.pool_size) fresh = (int64_t)at;
@@ -229,11 +260,11 @@ __device__ void merge_neighbour(const ElimArgs &A, int u, int wu, int iu, int v,
     const int ns = fits ? Jn + total : s;
     A.lsize[u] = ns;
     A.ljunk[u] = fits ? Jn : J;
-    const int h = __ldcg(A.height + u);
+    const int h = kPre ? m.h : __ldcg(A.height + u);
     const int hn = (hnow + 1 > h) ? hnow + 1 : h;
     A.height[u] = hn;
-    const int p = __ldcg(A.cpos + u);
-    if (p >= 0) {  // a remaining candidate of this cell: refresh its key in the leader CTA
+    const int p = kPre ? m.p : __ldcg(A.cpos + u);
+    if (p >= 0 && p < nslots) {  // a remaining candidate of this cell: refresh its key
       cand.deg[p] = ns;
       cand.third[p] = hn;
     }
@@ -390,11 +421,12 @@ __global__ void __launch_bounds__(512) elim_kernel(ElimArgs A) {
       }
       for (int i = rank * nw + wid; i < c; i += CS * nw) {
         const int u = aid[i];
-        if (__ldcg(A.lsize + u) - __ldcg(A.ljunk + u) > A.lmax) {
+        const NbrMeta m = load_meta<false>(A, u);
+        if (m.s - m.J > A.lmax) {
           if (lane == 0) set_err(A.err, kErrStaging);
           continue;
         }
-        merge_neighbour(A, u, aw[i], i, v, hnow, aid, aw, c, pid, pw, lane, lead);
+        merge_neighbour<false>(A, u, m, aw[i], i, v, hnow, aid, aw, c, pid, pw, lane, lead, k);
       }
     }
     cluster.sync();  // no CTA leaves while a peer may still read the leader's shared memory
@@ -411,28 +443,41 @@ __global__ void __launch_bounds__(512) elim_kernel(ElimArgs A) {
   }
 }
 
-// The global order over levels <= C for one graph, spread over the whole
-// GPU.  The cluster kernel above gives one cell at most 16 SMs; the global
-// order of a large graph is one long chain of eliminations whose neighbour
-// merges want all of them.  One cooperative launch, one block per SM, one
-// grid barrier per elimination.  Candidate keys live in global arrays at a
-// fixed index per candidate; block b owns the index slice [lo_b, hi_b): it
-// alone merges the lists of the candidates in its slice, refreshes their
-// keys and marks its picked candidate dead, so once its merges are done it
-// can take the argmin of its slice.  Per elimination:
-//   every block reduces the per-block argmins to the same pick v (the key
-//   order is strict); block 0 records it and writes back the previous pick's
+// Elimination over all SMs: one cooperative launch runs one or more cells,
+// each on its own range of blocks (one block per SM), without the cluster
+// kernel's limit of 16 SMs per cell.  The few large cells near the top of the
+// partition, and the global orders (one per graph), are long chains of
+// eliminations whose neighbour merges want more SMs than that.
+//
+// Ownership: block r of a cell's nb blocks owns the vertices u with
+// u mod nb == r.  It keeps the keys of the candidates it owns in shared
+// memory (their slots in cpos), merges the lists of the neighbours it owns
+// (candidates or not), refreshes their keys and retires its picked
+// candidate.  So a block finds its share of v's neighbours without a memory
+// round trip, and the argmin of its candidates reads only shared memory.
+// Per elimination:
+//   every block of the cell reduces the cell's per-block argmins to the same
+//   pick v (the key order is strict; the pick's height is its sum minus its
+//   degree); the first block records it and writes back the previous pick's
 //   compacted list (nobody reads that list any more); every block loads and
 //   compacts v's list into its shared memory (the same code as the cluster
-//   leader), merges those neighbours of v that fall in its slice, and writes
-//   the argmin of its slice                                  -- grid sync
-// Same key order, list rules and results as the cluster kernel in heap mode.
-struct HeapArgs {
-  ElimArgs E;          // heap_mode = 1; pstage (or shared memory) holds the per-warp merge buffers
-  int start, k;        // the cell: elim[start .. start + k)
-  int *cdeg, *ch, *cid;
-  unsigned char *dead;
-  int4 *partial;       // (deg + height, deg, id, index) per block
+//   leader), merges the neighbours of v it owns, and publishes the argmin of
+//   its candidates                                          -- cell barrier
+// The cell barrier is a monotonic arrival counter in global memory (barrier
+// t completes when it reaches t * nb); the launch is cooperative, so every
+// block is resident, and a wait is bounded (the block records kErrTimeout and
+// leaves).  Cells never wait on one another.  Same key order, list rules and
+// results as the cluster kernel in both modes: partition cells take the
+// first pick on stale keys and then refresh every key from the live lists; a
+// global order has live keys from the start and lets lists run empty.
+struct GridArgs {
+  ElimArgs E;              // cell_lo = the launch's first cell; pstage, when set, holds the per-warp merge buffers
+  const int *blk_cell;     // block -> cell of the launch (0-based)
+  const int *cell_blk0;    // cell -> its first block; entry ncell = the block count
+  int slice_max;           // most candidates one block owns (shared-memory key slots)
+  int4 *partial;           // (deg + height, deg, id, slot) per block
+  unsigned *bar;           // per cell: arrival counter
+  long long spin_limit;    // bound on one barrier wait, in SM clock cycles
 };
 
 __device__ __forceinline__ void better(int &bs, int &bd, int &bi, int &bp, int s, int d, int i, int p) {
@@ -453,90 +498,155 @@ __device__ __forceinline__ void block_best(int &bs, int &bd, int &bi, int &bp, i
     for (int w = 1; w < nw; w++) better(bs, bd, bi, bp, rs[w], rd[w], ri[w], rp[w]);
 }
 
-__global__ void __launch_bounds__(512, 1) heap_grid_kernel(HeapArgs H) {
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned *p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// Barrier t (target = t * nb) over the nb blocks of one cell.  False when the
+// wait ran out or another block recorded an error: the caller leaves.
+__device__ bool cell_barrier(unsigned *cnt, int nb, unsigned target, long long limit, int *err, int *s_flag) {
+  __syncthreads();
+  if (nb == 1) return true;
+  if (threadIdx.x == 0) {
+    int ok = 1;
+    __threadfence();  // this block's writes before its arrival
+    if (atomicAdd(cnt, 1u) + 1u == target) {
+      __threadfence();  // the other blocks' writes
+    } else {
+      const long long t0 = clock64();
+      while ((int)(ld_acquire_u32(cnt) - target) < 0) {
+        if (*(volatile int *)err != 0) { ok = 0; break; }
+        if (clock64() - t0 > limit) { set_err(err, kErrTimeout); ok = 0; break; }
+      }
+    }
+    *s_flag = ok;
+  }
+  __syncthreads();
+  return *s_flag != 0;
+}
+
+__global__ void __launch_bounds__(512, 1) cell_grid_kernel(GridArgs H) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ int s_rs[32], s_rd[32], s_ri[32], s_rp[32];
-  __shared__ int s_bc[4];  // v, height of the pick, |own list|, index of the pick
-  __shared__ int s_nmine;
-  cg::grid_group grid = cg::this_grid();
+  __shared__ int s_bc[4];  // v, height of the pick, |own list|, stop
+  __shared__ int4 s_best;  // this block's argmin (a one-block cell reads it here)
+  __shared__ int s_nmine, s_nslot, s_flag;
   const ElimArgs &A = H.E;
   const int tid = threadIdx.x, nthr = blockDim.x, lane = tid & 31, wid = tid >> 5, nw = nthr >> 5;
-  const int b = blockIdx.x, G = gridDim.x;
-  const int lal = (A.lmax + 3) & ~3;
+  const int b = blockIdx.x;
+  const int q = H.blk_cell[b];
+  const int f = H.cell_blk0[q], nb = H.cell_blk0[q + 1] - f, r = b - f;
+  const int start = A.cell_start[A.cell_lo + q], k = A.cell_count[A.cell_lo + q];
+  if (k == 0) return;  // the whole cell leaves; nobody waits on its barrier
+  unsigned *bar = H.bar + q;
+  unsigned bar_target = 0;
+  const int4 *partial = H.partial + f;
+  const int lal = (A.lmax + 3) & ~3, sal = (H.slice_max + 3) & ~3;
   int *aid = (int *)smem;
   int *aw = aid + lal;
   int *mine = aw + lal;    // indices into aid of the neighbours this block merges
+  int *cid = mine + lal;   // the candidates this block owns: id, degree key, height key, retired
+  int *cdeg = cid + sal;
+  int *ch = cdeg + sal;
+  int *dead = ch + sal;
   int *pid, *pw;           // this warp's merge buffers: shared memory when they fit, else global
   if (A.pstage) {
     pid = A.pstage + ((int64_t)b * nw + wid) * 2 * (int64_t)A.lmax;
     pw = pid + A.lmax;
   } else {
-    pid = mine + lal + (int64_t)wid * 2 * lal;
+    pid = dead + sal + (int64_t)wid * 2 * lal;
     pw = pid + lal;
   }
   Cand cand;
-  cand.id = H.cid;
-  cand.deg = H.cdeg;
-  cand.third = H.ch;
-  const int lo = (int)((int64_t)H.k * b / G), hi = (int)((int64_t)H.k * (b + 1) / G);
-  // keys of this block's slice, then its first argmin
-  for (int i = lo + tid; i < hi; i += nthr) {
-    const int v = A.elim[H.start + i];
-    H.cid[i] = v;
-    H.cdeg[i] = A.key_deg0[v];
-    H.ch[i] = A.key_h0[v];
-    H.dead[i] = 0;
-    A.cpos[v] = i;
+  cand.id = cid;
+  cand.deg = cdeg;
+  cand.third = ch;
+  // the candidates this block owns, with the first pick's keys (stale for a
+  // partition cell, prepared for a global order)
+  if (tid == 0) s_nslot = 0;
+  __syncthreads();
+  for (int i = tid; i < k; i += nthr) {
+    const int v = A.elim[start + i];
+    if (v % nb == r) {
+      const int t = atomicAdd(&s_nslot, 1);
+      if (t < H.slice_max) {
+        cid[t] = v;
+        cdeg[t] = A.key_deg0[v];
+        ch[t] = A.key_h0 ? A.key_h0[v] : 0;
+        dead[t] = 0;
+        A.cpos[v] = t;
+      }
+    }
   }
   __syncthreads();
-  {
-    int bs = INT_MAX, bd = INT_MAX, bi = INT_MAX, bp = -1;
-    for (int i = lo + tid; i < hi; i += nthr) {
-      const int d = H.cdeg[i];
-      better(bs, bd, bi, bp, d + H.ch[i], d, H.cid[i], i);
-    }
-    block_best(bs, bd, bi, bp, s_rs, s_rd, s_ri, s_rp);
-    if (tid == 0) H.partial[b] = make_int4(bs, bd, bi, bp);
+  const int ns = s_nslot;
+  if (ns > H.slice_max) {  // the host sized the slots from the same vertex set
+    if (tid == 0) set_err(A.err, kErrPick);
+    return;
   }
+  auto slice_best = [&]() {
+    int bs = INT_MAX, bd = INT_MAX, bi = INT_MAX, bp = -1;
+    for (int t = tid; t < ns; t += nthr)
+      if (!dead[t]) better(bs, bd, bi, bp, cdeg[t] + ch[t], cdeg[t], cid[t], t);
+    block_best(bs, bd, bi, bp, s_rs, s_rd, s_ri, s_rp);
+    if (tid == 0) {
+      s_best = make_int4(bs, bd, bi, bp);
+      if (nb > 1) H.partial[b] = s_best;
+    }
+  };
+  slice_best();
+  bar_target += nb;
+  if (!cell_barrier(bar, nb, bar_target, H.spin_limit, A.err, &s_flag)) return;
   int prev_v = -1, prev_c = 0;
-  grid.sync();
-  for (int j = 0; j < H.k; j++) {
+  for (int j = 0; j < k; j++) {
     // ---- the pick
     {
       int bs = INT_MAX, bd = INT_MAX, bi = INT_MAX, bp = -1;
-      for (int g = tid; g < G; g += nthr) {
-        const int4 q = __ldcg(H.partial + g);
-        better(bs, bd, bi, bp, q.x, q.y, q.z, q.w);
+      if (nb == 1) {
+        if (tid == 0) { bs = s_best.x; bd = s_best.y; bi = s_best.z; bp = s_best.w; }
+      } else {
+        for (int g = tid; g < nb; g += nthr) {
+          const int4 t = __ldcg(partial + g);
+          better(bs, bd, bi, bp, t.x, t.y, t.z, t.w);
+        }
+        block_best(bs, bd, bi, bp, s_rs, s_rd, s_ri, s_rp);
       }
-      block_best(bs, bd, bi, bp, s_rs, s_rd, s_ri, s_rp);
-      if (tid == 0) {  // bp >= 0: j < k candidates remain
-        s_bc[0] = bi;
-        s_bc[1] = __ldcg(H.ch + bp);
-        s_bc[3] = bp;
+      if (tid == 0) {
         s_nmine = 0;
-        if (b == 0) A.elim[H.start + j] = bi;
-        if (bp >= lo && bp < hi) {  // the owner retires the candidate
-          H.dead[bp] = 1;
-          A.cpos[bi] = -1;
+        s_bc[3] = bp < 0;  // j < k candidates remain, so a pick exists
+        if (bp >= 0) {
+          s_bc[0] = bi;
+          s_bc[1] = bs - bd;
+          if (r == 0) A.elim[start + j] = bi;
+          if (bi % nb == r) {  // the owner retires the candidate
+            dead[bp] = 1;
+            A.cpos[bi] = -1;
+          }
+        } else if (r == 0) {
+          set_err(A.err, kErrPick);
         }
       }
     }
-    // block 0: the previous pick's list, read by nobody since the barrier
-    if (b == 0 && prev_v >= 0) {
+    // the first block: the previous pick's list, read by nobody since the barrier
+    if (r == 0 && prev_v >= 0) {
       const int64_t off = __ldcg(A.slot_off + prev_v);
       for (int i = tid; i < prev_c; i += nthr) { A.slot_nbr[off + i] = aid[i]; A.slot_w[off + i] = aw[i]; }
       if (tid == 0) { A.lsize[prev_v] = prev_c; A.ljunk[prev_v] = 0; }
     }
     __syncthreads();
+    if (s_bc[3]) return;  // the same partials in every block of the cell: all leave
     const int v = s_bc[0], hnow = s_bc[1];
     const int64_t voff = __ldcg(A.slot_off + v);
     const int vJ = __ldcg(A.ljunk + v);
     const int sv = __ldcg(A.lsize + v) - vJ;
-    if (sv > A.lmax) {  // every block sees the same sizes: all leave together
-      if (b == 0 && tid == 0) set_err(A.err, kErrStaging);
+    if (sv > A.lmax) {  // every block of the cell sees the same sizes: all leave
+      if (r == 0 && tid == 0) set_err(A.err, kErrStaging);
       return;
     }
-    // ---- v's own list (every block the same copy)
+    // ---- v's own list, valid part (every block the same copy): merge
+    // duplicates, drop junk (kernel_functions.cu:338-361)
     for (int i = tid; i < sv; i += nthr) {
       aid[i] = __ldcg(A.slot_nbr + voff + vJ + i);
       aw[i] = __ldcg(A.slot_w + voff + vJ + i);
@@ -558,43 +668,50 @@ __global__ void __launch_bounds__(512, 1) heap_grid_kernel(HeapArgs H) {
         c = 0;
         for (int i = 0; i < sv; i++) if (aid[i] != INT_MAX) { aid[c] = aid[i]; aw[c] = aw[i]; c++; }
       }
+      if (c == 0 && !A.heap_mode) {  // a partition cell never eliminates an isolated vertex
+        if (r == 0) set_err(A.err, kErrEmpty);
+        s_bc[3] = 1;
+      }
       s_bc[2] = c;
     }
     __syncthreads();
+    if (s_bc[3]) return;
     const int c = s_bc[2];
-    // ---- the neighbours in this block's slice
-    for (int i = tid; i < c; i += nthr) {
-      const int p = __ldcg(A.cpos + aid[i]);
-      if ((p >= lo && p < hi) || (p < 0 && b == 0)) mine[atomicAdd(&s_nmine, 1)] = i;
-    }
+    // ---- the neighbours this block owns
+    for (int i = tid; i < c; i += nthr)
+      if (aid[i] % nb == r) mine[atomicAdd(&s_nmine, 1)] = i;
     __syncthreads();
     const int nm = s_nmine;
     for (int t = wid; t < nm; t += nw) {
       const int i = mine[t];
       const int u = aid[i];
-      if (__ldcg(A.lsize + u) - __ldcg(A.ljunk + u) > A.lmax) {
+      const NbrMeta m = load_meta<true>(A, u);
+      if (m.s - m.J > A.lmax) {
         if (lane == 0) set_err(A.err, kErrStaging);
         continue;
       }
-      merge_neighbour(A, u, aw[i], i, v, hnow, aid, aw, c, pid, pw, lane, cand);
+      merge_neighbour<true>(A, u, m, aw[i], i, v, hnow, aid, aw, c, pid, pw, lane, cand, ns);
     }
     __syncthreads();
-    // ---- the argmin of this block's slice, keys final (only this block writes them)
-    {
-      int bs = INT_MAX, bd = INT_MAX, bi = INT_MAX, bp = -1;
-      for (int i = lo + tid; i < hi; i += nthr)
-        if (!H.dead[i]) {
-          const int d = __ldcg(H.cdeg + i);
-          better(bs, bd, bi, bp, d + __ldcg(H.ch + i), d, H.cid[i], i);
+    // ---- after the first pick of a partition cell every key becomes live
+    // (kernel_functions.cu:471-475); this block alone wrote its candidates' lists
+    if (j == 0 && !A.heap_mode) {
+      for (int t = tid; t < ns; t += nthr)
+        if (!dead[t]) {
+          const int u = cid[t];
+          cdeg[t] = __ldcg(A.lsize + u);
+          ch[t] = __ldcg(A.height + u);
         }
-      block_best(bs, bd, bi, bp, s_rs, s_rd, s_ri, s_rp);
-      if (tid == 0) H.partial[b] = make_int4(bs, bd, bi, bp);
+      __syncthreads();
     }
+    // ---- the argmin of this block's candidates, keys final
+    slice_best();
     prev_v = v;
     prev_c = c;
-    grid.sync();
+    bar_target += nb;
+    if (!cell_barrier(bar, nb, bar_target, H.spin_limit, A.err, &s_flag)) return;
   }
-  if (b == 0 && prev_v >= 0) {
+  if (r == 0 && prev_v >= 0) {
     const int64_t off = __ldcg(A.slot_off + prev_v);
     for (int i = tid; i < prev_c; i += nthr) { A.slot_nbr[off + i] = aid[i]; A.slot_w[off + i] = aw[i]; }
     if (tid == 0) { A.lsize[prev_v] = prev_c; A.ljunk[prev_v] = 0; }
@@ -904,8 +1021,11 @@ ElimPlan::ElimPlan(const std::vector<Graph *> &graphs) : gs(graphs) {
   // graph.  Within a step, cells are grouped by size class, each group is a
   // launch with its own cluster size (a large cell spreads its merges over up
   // to 16 CTAs), and the groups of a step run side by side on forked streams.
+  // A step with few cells (or the global orders) instead runs as one
+  // cooperative launch of cell_grid_kernel over all SMs.
   const int smem_dyn = enable_max_dynamic_smem(elim_kernel);
-  const int smem_dyn_hg = enable_max_dynamic_smem(heap_grid_kernel);
+  const int smem_dyn_g = enable_max_dynamic_smem(cell_grid_kernel);
+  const bool force_cluster = std::getenv("GPUH2H_CLUSTER_HEAP") != nullptr;
   GH_CUDA(cudaFuncSetAttribute(elim_kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
   int dev = 0;
   GH_CUDA(cudaGetDevice(&dev));
@@ -949,10 +1069,111 @@ ElimPlan::ElimPlan(const std::vector<Graph *> &graphs) : gs(graphs) {
   const int nsteps = (int)step_cells.size();
   std::vector<int> fcs, fcc;
   auto al = [](int64_t bb) { return (bb + 15) & ~int64_t(15); };
-  int64_t pstage_ints = 0;
+  int64_t pstage_ints = 0, partial_max = 0;
+  std::vector<int> gmap;
+  // Whole-step cooperative launch: one block per SM.  Taken by default for a
+  // step of one cell -- the global order of a single graph, one long chain
+  // that the cluster kernel would give 16 SMs (1.5x faster on road graphs).
+  // Measured on road graphs, steps of several cells run faster on clusters:
+  // at 1 block of 4-16 warps per SM the cooperative kernel has fewer merge
+  // warps per cell than the cluster kernel's several CTAs per SM, and its
+  // barrier goes through L2.  GPUH2H_GRID_CELLS (most cells a cooperative
+  // launch takes) overrides.  Blocks go to cells greedily by an estimate of
+  // the chain time, eliminations x (1 + merge rounds x list length), merge
+  // rounds ~ 2 x list bound / warps.
+  auto grid_launch = [&](const std::vector<Cell> &cells, int st, bool heap) -> bool {
+    const int ncell = (int)cells.size();
+    int max_cells = 1;
+    if (const char *e = std::getenv("GPUH2H_GRID_CELLS")) max_cells = std::atoi(e);
+    if (force_cluster || ncell > max_cells || ncell > nsm) return false;
+    int lmax = 1, kmax = 1;
+    for (const Cell &c : cells) {
+      lmax = std::max(lmax, c.lbound);
+      kmax = std::max(kmax, c.count);
+    }
+    // blocks per cell (16 warps each; the estimate only ranks cells)
+    std::vector<int> nb(ncell, 1);
+    auto est = [&](int c, int b) {
+      const double lb = cells[c].lbound;
+      return cells[c].count * (1.0 + std::max(1.0, 2.0 * lb / ((double)b * 16)) * (1.0 + lb / 256.0));
+    };
+    std::priority_queue<std::pair<double, int>> pq;
+    for (int c = 0; c < ncell; c++) pq.push({est(c, 1), c});
+    int used = ncell;
+    while (used < nsm && !pq.empty()) {
+      const auto [e, c] = pq.top();
+      pq.pop();
+      if (est(c, nb[c] + 1) >= e) continue;  // more blocks would not shorten this chain
+      nb[c]++;
+      used++;
+      pq.push({est(c, nb[c]), c});
+    }
+    // candidate slots: block r of cell c owns the cell's vertices v with v mod nb == r
+    int slice_max = 1;
+    {
+      std::vector<int> cnt;
+      for (int c = 0; c < ncell; c++) {
+        cnt.assign(nb[c], 0);
+        for (int i = 0; i < cells[c].count; i++) cnt[f_elim[cells[c].start + i] % nb[c]]++;
+        for (int x : cnt) slice_max = std::max(slice_max, x);
+      }
+      int64_t arrivals = 0;
+      for (int c = 0; c < ncell; c++) arrivals = std::max<int64_t>(arrivals, (int64_t)(cells[c].count + 1) * nb[c]);
+      if (arrivals >= INT32_MAX) return false;  // the barrier counter compares as int
+    }
+    const int64_t own = 3 * al(4LL * lmax) + 4 * al(4LL * slice_max), per_warp = 2 * al(4LL * lmax);
+    if (own > smem_dyn_g) return false;
+    // per-warp merge buffers in shared memory when 4+ warps' worth fit (a
+    // merge walks them serially), else 16 warps with buffers in global memory
+    const int64_t fit = (smem_dyn_g - own) / per_warp;
+    const int hw = fit >= 4 ? (int)std::min<int64_t>(16, fit) : 16;
+    const bool gstage = fit < 4;
+    const int64_t hsmem = gstage ? own : own + hw * per_warp;
+    int per = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, cell_grid_kernel, hw * 32, (size_t)hsmem) !=
+            cudaSuccess ||
+        per < 1) {
+      cudaGetLastError();
+      return false;
+    }
+    Launch Lc;
+    Lc.step = st;
+    Lc.level = step_level[st];
+    Lc.heap = heap;
+    Lc.lo = (int64_t)fcs.size();
+    Lc.ncell = ncell;
+    Lc.kmax = kmax;
+    Lc.lmax = lmax;
+    Lc.cs = 1;
+    Lc.nw = hw;
+    Lc.slots = used;
+    Lc.smem = hsmem;
+    Lc.global_stage = gstage;
+    Lc.pstage_off = 0;
+    Lc.grid = true;
+    Lc.slice_max = slice_max;
+    Lc.map_off = (int64_t)gmap.size();
+    Lc.bar_off = grid_bar_words;
+    for (const Cell &c : cells) {
+      fcs.push_back(c.start);
+      fcc.push_back(c.count);
+    }
+    for (int c = 0; c < ncell; c++)
+      for (int i = 0; i < nb[c]; i++) gmap.push_back(c);
+    for (int c = 0, b0 = 0; c <= ncell; c++) {
+      gmap.push_back(b0);
+      if (c < ncell) b0 += nb[c];
+    }
+    grid_bar_words += ncell;
+    partial_max = std::max<int64_t>(partial_max, used);
+    if (gstage) pstage_ints = std::max(pstage_ints, (int64_t)used * hw * 2 * (int64_t)lmax);
+    launches.push_back(Lc);
+    return true;
+  };
   for (int st = 0; st < nsteps; st++) {
     const bool heap = st == nsteps - 1;
     std::vector<Cell> &cells = step_cells[st];
+    if (grid_launch(cells, st, heap)) continue;
     std::stable_sort(cells.begin(), cells.end(), [](const Cell &x, const Cell &y) { return x.cls > y.cls; });
     int64_t step_pstage = 0;
     for (size_t g0 = 0; g0 < cells.size();) {
@@ -1021,41 +1242,16 @@ ElimPlan::ElimPlan(const std::vector<Graph *> &graphs) : gs(graphs) {
         cudaGetLastError();
       }
       Lc.cs = cs;
-      Lc.grid_heap = false;
-      if (heap && Lc.ncell == 1 && K == 1 && !std::getenv("GPUH2H_CLUSTER_HEAP")) {
-        // one graph's global order: all SMs in one cooperative launch when
-        // the eliminated list fits shared memory; per-warp merge buffers in
-        // shared memory too when 4+ warps' worth fit (a merge walks them
-        // serially), else 16 warps with buffers in global memory
-        const int64_t own = 3 * al(4LL * Lc.lmax), per_warp = 2 * al(4LL * Lc.lmax);
-        const int64_t fit = own <= smem_dyn_hg ? (smem_dyn_hg - own) / per_warp : 0;
-        const int hw = fit >= 4 ? (int)std::min<int64_t>(16, fit) : 16;
-        const int64_t hsmem = fit >= 4 ? own + hw * per_warp : own;
-        int per = 0;
-        if (own <= smem_dyn_hg &&
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, heap_grid_kernel, hw * 32, (size_t)hsmem) ==
-                cudaSuccess &&
-            per >= 1) {
-          Lc.grid_heap = true;
-          Lc.cs = 1;
-          Lc.nw = hw;
-          Lc.smem = hsmem;
-          Lc.global_stage = fit < 4;
-        }
-        cudaGetLastError();
-      }
+      Lc.grid = false;
+      Lc.slice_max = 0;
+      Lc.map_off = Lc.bar_off = 0;
       Lc.pstage_off = step_pstage;
-      if (Lc.grid_heap) {
-        if (Lc.global_stage) step_pstage += (int64_t)nsm * Lc.nw * 2 * (int64_t)Lc.lmax;
-      }
-      else if (Lc.global_stage) step_pstage += (int64_t)Lc.ncell * cs * nw * 2 * (int64_t)Lc.lmax;
+      if (Lc.global_stage) step_pstage += (int64_t)Lc.ncell * cs * nw * 2 * (int64_t)Lc.lmax;
       launches.push_back(Lc);
       g0 = g1;
     }
     pstage_ints = std::max(pstage_ints, step_pstage);
   }
-  heap_cell_start = fcs.empty() ? 0 : fcs.back();
-  heap_cell_count = fcc.empty() ? 0 : fcc.back();
   {
     // side streams for the groups of a step beyond the first
     int most = 1;
@@ -1093,14 +1289,12 @@ ElimPlan::ElimPlan(const std::vector<Graph *> &graphs) : gs(graphs) {
     adj_w = palloc<int>(std::max<int64_t>(M, 1), bytes);
     heap_verts = palloc<int>(std::max(heap_total, 1), bytes);
     if (pstage_ints) pstage = palloc<int>(pstage_ints, bytes);
-    for (const Launch &Lc : launches)
-      if (Lc.grid_heap) {
-        hg_deg = palloc<int>(Lc.kmax, bytes);
-        hg_h = palloc<int>(Lc.kmax, bytes);
-        hg_id = palloc<int>(Lc.kmax, bytes);
-        hg_dead = palloc<unsigned char>(Lc.kmax, bytes);
-        hg_partial = palloc<int4>(nsm, bytes);
-      }
+    if (!gmap.empty()) {
+      hg_partial = palloc<int4>(partial_max, bytes);
+      grid_map = palloc<int>(gmap.size(), bytes);
+      grid_bar = palloc<unsigned>(grid_bar_words, bytes);
+      GH_CUDA(cudaMemcpy(grid_map, gmap.data(), sizeof(int) * gmap.size(), cudaMemcpyHostToDevice));
+    }
     for (int k = 1; k < max_group; k++) {
       cudaStream_t st = nullptr;
       cudaEvent_t e = nullptr;
@@ -1136,10 +1330,12 @@ void ElimPlan::release() {
                 elim_init, deg0, deg_init, h0, cpos, err, ljunk, cell_start, cell_count, adj_off, adj_v, adj_w,
                 heap_verts, pstage};
   for (void *p : ps) cudaFree(p);
-  cudaFree(hg_deg); cudaFree(hg_h); cudaFree(hg_id); cudaFree(hg_dead); cudaFree(hg_partial);
-  hg_deg = hg_h = hg_id = nullptr;
-  hg_dead = nullptr;
+  cudaFree(hg_partial);
+  cudaFree(grid_map);
+  cudaFree(grid_bar);
+  grid_map = nullptr;
   hg_partial = nullptr;
+  grid_bar = nullptr;
   cudaFree(rank);
   cudaFree(father_dev);
   rank = father_dev = nullptr;
@@ -1184,21 +1380,15 @@ void ElimPlan::launch_one(const Launch &Lc, cudaStream_t s, bool trace) {
   cfg.stream = s;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   if (trace) { cudaEventCreate(&ev0); cudaEventCreate(&ev1); cudaEventRecord(ev0, s); }
-  if (Lc.grid_heap) {
-    HeapArgs H;
+  if (Lc.grid) {
+    GridArgs H;
     H.E = A;
-    H.start = 0;
-    H.k = 0;
-    {
-      // the heap cell's start and size (host copies of the cell table entry)
-      H.start = heap_cell_start;
-      H.k = heap_cell_count;
-    }
-    H.cdeg = hg_deg;
-    H.ch = hg_h;
-    H.cid = hg_id;
-    H.dead = hg_dead;
+    H.blk_cell = grid_map + Lc.map_off;
+    H.cell_blk0 = grid_map + Lc.map_off + Lc.slots;
+    H.slice_max = Lc.slice_max;
     H.partial = (int4 *)hg_partial;
+    H.bar = grid_bar + Lc.bar_off;
+    H.spin_limit = spin_limit_cycles();
     cudaLaunchAttribute ca[1];
     ca[0].id = cudaLaunchAttributeCooperative;
     ca[0].val.cooperative = 1;
@@ -1206,10 +1396,10 @@ void ElimPlan::launch_one(const Launch &Lc, cudaStream_t s, bool trace) {
     cc.attrs = ca;
     cc.numAttrs = 1;
     cc.blockDim = dim3(Lc.nw * 32);
-    cc.gridDim = dim3(nsm);
+    cc.gridDim = dim3(Lc.slots);
     cc.dynamicSmemBytes = (size_t)Lc.smem;
     cc.stream = s;
-    if (H.k > 0) GH_CUDA(cudaLaunchKernelEx(&cc, heap_grid_kernel, H));
+    GH_CUDA(cudaLaunchKernelEx(&cc, cell_grid_kernel, H));
   } else {
     GH_CUDA(cudaLaunchKernelEx(&cfg, elim_kernel, A));
   }
@@ -1221,7 +1411,7 @@ void ElimPlan::launch_one(const Launch &Lc, cudaStream_t s, bool trace) {
     std::fprintf(stderr,
                  "[gpuh2h] elim %s %d: %d cells x %d CTAs x %d warps, kmax %d, lmax %d, smem %lld, slots %d%s%s: %.3f ms\n",
                  Lc.heap ? "heap" : "level", Lc.level, Lc.ncell, Lc.cs, Lc.nw, Lc.kmax, Lc.lmax, (long long)Lc.smem,
-                 Lc.slots, Lc.global_stage ? " (global merge staging)" : "", Lc.grid_heap ? " (all SMs)" : "", ms);
+                 Lc.slots, Lc.global_stage ? " (global merge staging)" : "", Lc.grid ? " (cooperative, slots = blocks)" : "", ms);
     cudaEventDestroy(ev0);
     cudaEventDestroy(ev1);
   }
@@ -1240,6 +1430,7 @@ void ElimPlan::enqueue(cudaStream_t s, cudaEvent_t *heap_ev, bool trace) {
   GH_CUDA(cudaMemsetAsync(ljunk, 0, sizeof(int) * N, s));
   GH_CUDA(cudaMemsetAsync(cpos, 0xff, sizeof(int) * N, s));  // -1
   GH_CUDA(cudaMemsetAsync(err, 0, sizeof(int), s));
+  if (grid_bar_words) GH_CUDA(cudaMemsetAsync(grid_bar, 0, sizeof(unsigned) * grid_bar_words, s));
   scatter_adjacency_kernel<<<std::max(1, std::min(4096, (N + 255) / 256)), 256, 0, s>>>(
       adj_off, adj_v, adj_w, slot_off, slot_nbr, slot_w, N);
   GH_CUDA(cudaGetLastError());
@@ -1279,7 +1470,9 @@ void ElimPlan::check_error() {
   GH_CHECK(e == 0, H2H_ERR_DEVICE,
            e == kErrOverflow ? "contraction: a list outgrew its LUB capacity"
            : e == kErrEmpty  ? "contraction: eliminated a vertex with an empty list (disconnected input)"
-                             : "contraction: a list outgrew the staging bound");
+           : e == kErrTimeout ? "contraction: a cell barrier wait ran out"
+           : e == kErrPick    ? "contraction: no candidate left to pick"
+                              : "contraction: a list outgrew the staging bound");
 }
 
 void ElimPlan::build_lists() {

@@ -132,7 +132,13 @@ struct ElimPlan {
     int step, level, ncell, kmax, lmax, cs, nw, slots;
     int64_t lo, smem, pstage_off;
     bool heap, global_stage;
-    bool grid_heap;  // the global order of one graph as one cooperative launch over all SMs
+    // cell_grid_kernel: the step's cells in one cooperative launch, `slots`
+    // blocks (block -> cell map at grid_map + map_off, cell -> first block
+    // after it), one barrier counter per cell at grid_bar + bar_off, at most
+    // slice_max candidates owned by one block
+    bool grid;
+    int slice_max;
+    int64_t map_off, bar_off;
   };
   std::vector<Graph *> gs;
   std::vector<int> vbase;
@@ -154,11 +160,11 @@ struct ElimPlan {
   unsigned long long *pool_next = nullptr, *pool_first = nullptr;
   ListStore lists;       // compact final lists (forest numbering), after build_lists()
   int *rank = nullptr, *father_dev = nullptr;
-  // candidate keys of the whole-GPU global order (heap_grid_kernel)
-  int *hg_deg = nullptr, *hg_h = nullptr, *hg_id = nullptr;
-  unsigned char *hg_dead = nullptr;
+  // cell_grid_kernel state: per-block argmins, block maps, barrier counters
+  int *grid_map = nullptr;
   void *hg_partial = nullptr;
-  int heap_cell_start = 0, heap_cell_count = 0;  // the last cell of the table (one graph: its global order)
+  unsigned *grid_bar = nullptr;
+  int64_t grid_bar_words = 0;
   int64_t bytes = 0;
   explicit ElimPlan(const std::vector<Graph *> &graphs);
   ~ElimPlan();

@@ -195,14 +195,6 @@ __global__ void fill_level_kernel(FillArgs A) {
 // than the light edges above it, so O(log n)), staged in shared memory; a
 // short search finds the segment holding depth j+1 and the path array gives
 // the node.  No per-node ancestor list is stored.
-//
-// Bound on one dependency wait, in SM clock cycles: 2 s at 2 GHz, or
-// GPUH2H_SPIN_LIMIT_MS (profilers replay instrumented kernels much slower).
-long long spin_limit_cycles() {
-  long long ms = 2000;
-  if (const char *e = std::getenv("GPUH2H_SPIN_LIMIT_MS")) ms = std::max(1LL, std::atoll(e));
-  return ms * 2000000LL;
-}
 
 struct FlowArgs {
   // tiles in forest BFS order: ticket t belongs to node tile_node[t]; the

@@ -60,8 +60,13 @@ def batch_specs(tmp_path_factory):
     return root, specs
 
 
-def test_batch_matches_single_builds(batch_specs):
+@pytest.mark.parametrize("grid_cells", [None, "0", "100000"])
+def test_batch_matches_single_builds(batch_specs, monkeypatch, grid_cells):
+    """Default launch shapes; every step on clusters; every step (all graphs'
+    cells, global orders included) as one cooperative launch."""
     import gpuh2h
+    if grid_cells is not None:
+        monkeypatch.setenv("GPUH2H_GRID_CELLS", grid_cells)
     _, specs = batch_specs
     graphs = [gpuh2h.Graph("b", H, C, 4, 1, files=f) for f, H, C in specs]
     b = gpuh2h.Batch(graphs, threads=4)
