@@ -113,7 +113,7 @@ def batched_build(threads: int, count: int) -> dict:
     # (our dataflow fill, and the reference's level-by-level mapping)
     plain_ms, plain_bad = 0.0, 0
     for gs in seq:
-        ms, bad = gs.fill_labels_plain()
+        ms, bad = gs.fill_labels_plain("pair")
         plain_ms += ms
         plain_bad += bad
     assert plain_bad == 0, "the plain fill mapping disagrees with the labels"
@@ -513,6 +513,8 @@ def main():
     ap.add_argument("--latency-batches", type=int, default=200)
     ap.add_argument("--cpu-budget", type=float, default=10.0, help="seconds of CPU query work for cpu_baseline")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--plain-node-fill", action="store_true",
+                    help="also time the reference's node-per-thread fill mapping (about a minute)")
     ap.add_argument("--batch-graphs", type=int, default=64, help="graphs of the batched-build measurement (0: skip)")
     ap.add_argument("--serve", action="store_true", help="run the serving measurement instead")
     ap.add_argument("--large", action="store_true", help="run the 3.6M-vertex single-graph measurement instead")
@@ -666,7 +668,7 @@ def main():
     # L4 fill: own rows read+written, separator lists, one ancestor entry per update
     fill_s = info["t_fill_gpu_us"] / 1e6
     fill_bytes = 8 * info["label_size"] + 8 * info["pos_size"] + 4 * info["label_updates"]
-    plain_fill_ms, plain_fill_bad = g.fill_labels_plain()
+    plain_fill_ms, plain_fill_bad = g.fill_labels_plain("pair")
     assert plain_fill_bad == 0, "the plain fill mapping disagrees with the labels"
     fill = {"kernel": "fill_flow_kernel", "updates": info["label_updates"], "seconds": fill_s,
             "plain_gpu_seconds": plain_fill_ms / 1e3,
@@ -675,6 +677,13 @@ def main():
             "algorithmic_bytes": fill_bytes,
             "achieved_gbs": fill_bytes / fill_s / 1e9 if fill_s > 0 else None,
             "frac_of_hbm": fill_bytes / fill_s / 1e9 / peak if fill_s > 0 else None}
+    if args.plain_node_fill:
+        # the reference's parallelFine=1 mapping: a minute on this graph, so only on request
+        node_fill_ms, node_fill_bad = g.fill_labels_plain("node")
+        assert node_fill_bad == 0, "the node-per-thread fill mapping disagrees with the labels"
+        fill.update({"plain_node_gpu_seconds": node_fill_ms / 1e3,
+                     "plain_node_gpu": "the reference's parallelFine=1 mapping: one thread per node, one launch + "
+                                       "sync per tree level"})
     line = {
         "metric": METRIC, "value": value, "unit": "queries/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1000.0 * t_max / args.steps, "higher_is_better": True,

@@ -194,7 +194,12 @@ int h2h_query_batch_plain(const h2h_graph *h, const int *x_dev, const int *y_dev
 
 int h2h_fill_labels_plain(const h2h_graph *h, double *ms, int64_t *mismatches) {
   if (!h) { gh::set_last_error("null handle"); return H2H_ERR_ARG; }
-  return guarded([&] { gh::fill_labels_plain(h->g, ms, mismatches); });
+  return guarded([&] { gh::fill_labels_plain(h->g, 0, ms, mismatches); });
+}
+
+int h2h_fill_labels_plain_node(const h2h_graph *h, double *ms, int64_t *mismatches) {
+  if (!h) { gh::set_last_error("null handle"); return H2H_ERR_ARG; }
+  return guarded([&] { gh::fill_labels_plain(h->g, 1, ms, mismatches); });
 }
 
 int h2h_query_batch_host(const h2h_graph *hc, const int *x, const int *y, int *out, int64_t n, int mode) {

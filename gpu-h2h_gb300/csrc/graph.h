@@ -266,7 +266,7 @@ inline bool uses_level_fill(const Graph &g) {
 void download_labels(const Graph &g, int *dis_out);    // labels.cu, reference layout
 // labels.cu: the reference's level-by-level GPU fill mapping on a built L4
 // graph (measurement baseline): device ms and mismatches against the labels
-void fill_labels_plain(const Graph &g, double *ms, int64_t *mismatches);
+void fill_labels_plain(const Graph &g, int mapping, double *ms, int64_t *mismatches);
 // labels.cu: the graph's position lists (reference layout, graph-local ids)
 void download_positions(const Graph &g, int *pos_id, int *pos_pos);
 // contract.cu: host copies of the X lists (graph-local ids) from the device

@@ -17,8 +17,9 @@
 //     the node's row stays in shared memory, and its ancestors' row offsets
 //     are staged from the father's, which the previous level wrote to a
 //     ping-pong buffer;
-//   * plain_fill_level_kernel, the reference's own mapping (one thread per
-//     (v, u) pair, a launch per level), kept as a measurement baseline.
+//   * plain_fill_level_kernel and plain_node_fill_kernel, the reference's own
+//     two GPU mappings (one thread per (v, u) pair, or one per node; a launch
+//     per level), kept as measurement baselines.
 //
 // Rows are padded to 16-byte starts (drow[v] is a multiple of 4 ints) so the
 // u-row reads are 128-bit vector loads.
@@ -365,6 +366,38 @@ __global__ void plain_fill_level_kernel(const int *pair_v, const int64_t *pair_k
     for (int j = d - 2; j > p && a >= 0; j--) {
       atomicMin(dis + base + j, t + __ldcg(dis + drow[a] + p));
       a = father[a];
+    }
+  }
+}
+
+// The reference's other GPU fill mapping (parallelFine = 1:
+// makeH2HLabel_noCommunication_D_noHub, kernel_functions.cu:802-837, with its
+// commented L4 block enabled), kept as a measurement baseline: one thread per
+// node of one tree level, walking the node's position list from the highest
+// position down (its own entry, the last, excluded); each entry u at position
+// p min-updates the columns below p from u's row and, for L4, the columns
+// above p from the ancestors' column p along the father chain.  The thread
+// owns its row: no atomics.
+__global__ void plain_node_fill_kernel(const int *nodes, int cnt, const int64_t *drow, const int *depth,
+                                       const int *father, const int64_t *pos_hash, const int *pos_pos,
+                                       const int *pos_id, const int *pos_w, int *dis) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += gridDim.x * blockDim.x) {
+    const int v = nodes[i];
+    const int64_t base = drow[v];
+    const int d = depth[v];
+    for (int64_t k = pos_hash[v + 1] - 1; k >= pos_hash[v]; k--) {
+      const int u = pos_id[k];
+      if (u == v) continue;
+      const int p = pos_pos[k];
+      const int t = dis[base + p];
+      const int64_t ub = drow[u];
+      for (int j = p - 1; j >= 0; j--) dis[base + j] = min(dis[base + j], t + __ldcg(dis + ub + j));
+      int a = v;
+      for (int j = d - 2; j > p; j--) {
+        a = father[a];
+        if (a < 0) break;
+        dis[base + j] = min(dis[base + j], t + __ldcg(dis + drow[a] + p));
+      }
     }
   }
 }
@@ -1196,11 +1229,14 @@ void upload_labels(Graph &g, const std::vector<int> &dis, const std::vector<int>
   g.drow_host.swap(drow);
 }
 
-// Runs the reference's mapping (plain_fill_level_kernel) on the built graph
-// into a scratch copy of the rows and compares it with the built labels.
-// The device time of the per-level launches and synchronisations goes to
-// *ms; *mismatches receives the number of differing entries.
-void fill_labels_plain(const Graph &g, double *ms, int64_t *mismatches) {
+// Runs one of the reference's GPU fill mappings (mapping 0: a thread per
+// (v, u) pair, plain_fill_level_kernel; 1: a thread per node,
+// plain_node_fill_kernel) on the built graph into a scratch copy of the rows
+// and compares it with the built labels.  The device time of the per-level
+// launches and synchronisations goes to *ms; *mismatches receives the number
+// of differing entries.
+void fill_labels_plain(const Graph &g, int mapping, double *ms, int64_t *mismatches) {
+  GH_CHECK(mapping == 0 || mapping == 1, H2H_ERR_ARG, "mapping must be 0 (pair per thread) or 1 (node per thread)");
   GH_CHECK(g.labelled && g.label_mode == H2H_LABEL_L4, H2H_ERR_STATE, "needs built L4 labels");
   const DeviceIndex &D = g.dev;
   const int n = g.n;
@@ -1223,13 +1259,14 @@ void fill_labels_plain(const Graph &g, double *ms, int64_t *mismatches) {
   int64_t tmp = 0;
   int *d_dis = nullptr, *d_pv = nullptr, *d_w = nullptr;
   int64_t *d_pk = nullptr, *d_drow = nullptr;
-  int *d_depth = nullptr, *d_father = nullptr, *d_pos_pos = nullptr, *d_pos_id = nullptr;
+  int *d_depth = nullptr, *d_father = nullptr, *d_pos_pos = nullptr, *d_pos_id = nullptr, *d_bfs = nullptr;
   int64_t *d_pos_hash = nullptr;
   unsigned long long *d_bad = nullptr;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   auto cleanup = [&]() {
     cudaFree(d_dis); cudaFree(d_pv); cudaFree(d_w); cudaFree(d_pk); cudaFree(d_drow); cudaFree(d_depth);
     cudaFree(d_father); cudaFree(d_pos_pos); cudaFree(d_pos_id); cudaFree(d_pos_hash); cudaFree(d_bad);
+    cudaFree(d_bfs);
     if (e0) cudaEventDestroy(e0);
     if (e1) cudaEventDestroy(e1);
   };
@@ -1265,6 +1302,9 @@ void fill_labels_plain(const Graph &g, double *ms, int64_t *mismatches) {
     d_w = dalloc<int>(std::max<int64_t>(np, 1), tmp);
     d_pos_hash = dalloc<int64_t>(n + 1, tmp);
     d_bad = dalloc<unsigned long long>(1, tmp);
+    d_bfs = dalloc<int>(std::max<size_t>(g.tree_bfs.size(), 1), tmp);
+    if (!g.tree_bfs.empty())
+      GH_CUDA(cudaMemcpy(d_bfs, g.tree_bfs.data(), sizeof(int) * g.tree_bfs.size(), cudaMemcpyHostToDevice));
     if (!pv.empty()) {
       GH_CUDA(cudaMemcpy(d_pv, pv.data(), sizeof(int) * pv.size(), cudaMemcpyHostToDevice));
       GH_CUDA(cudaMemcpy(d_pk, pk.data(), sizeof(int64_t) * pk.size(), cudaMemcpyHostToDevice));
@@ -1286,11 +1326,18 @@ void fill_labels_plain(const Graph &g, double *ms, int64_t *mismatches) {
     GH_CUDA(cudaGetLastError());
     GH_CUDA(cudaDeviceSynchronize());
     for (int l = 1; l < nlev; l++) {
-      const int64_t a = lvl_off[l], b = lvl_off[l + 1];
-      if (b == a) continue;
-      const int cnt = (int)(b - a);
-      plain_fill_level_kernel<<<(cnt + 255) / 256, 256>>>(d_pv + a, d_pk + a, cnt, d_drow, d_depth, d_father,
-                                                           d_pos_pos, d_pos_id, d_w, d_dis);
+      if (mapping == 1) {
+        const int cnt = g.tree_hash[l + 1] - g.tree_hash[l];
+        if (cnt == 0) continue;
+        plain_node_fill_kernel<<<(cnt + 255) / 256, 256>>>(d_bfs + g.tree_hash[l], cnt, d_drow, d_depth, d_father,
+                                                            d_pos_hash, d_pos_pos, d_pos_id, d_w, d_dis);
+      } else {
+        const int64_t a = lvl_off[l], b = lvl_off[l + 1];
+        if (b == a) continue;
+        const int cnt = (int)(b - a);
+        plain_fill_level_kernel<<<(cnt + 255) / 256, 256>>>(d_pv + a, d_pk + a, cnt, d_drow, d_depth, d_father,
+                                                             d_pos_pos, d_pos_id, d_w, d_dis);
+      }
       GH_CUDA(cudaGetLastError());
       GH_CUDA(cudaDeviceSynchronize());
     }

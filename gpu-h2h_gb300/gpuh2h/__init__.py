@@ -110,6 +110,7 @@ SIGNATURES = {
     "h2h_copy_input_arcs": (_i32, [_vp, _vp, _vp, _vp]),
     "h2h_save_index": (_i32, [_vp, _cp]),
     "h2h_fill_labels_plain": (_i32, [_vp, C.POINTER(C.c_double), C.POINTER(_i64)]),
+    "h2h_fill_labels_plain_node": (_i32, [_vp, C.POINTER(C.c_double), C.POINTER(_i64)]),
     "h2h_load_index": (_i32, [_cp, C.POINTER(_vp)]),
     "h2h_batch_build": (_i32, [_vp, _i32, _i32, C.POINTER(_vp)]),
     "h2h_batch_set_weights": (_i32, [_vp, _i32, _vp]),
@@ -216,12 +217,15 @@ class Graph:
         g.graphName = graphName
         return g
 
-    def fill_labels_plain(self):
-        """(device ms, mismatching entries) of the reference's fill mapping
-        re-run on this graph (measurement baseline)."""
+    def fill_labels_plain(self, mapping: str = "pair"):
+        """(device ms, mismatching entries) of one of the reference's GPU fill
+        mappings re-run on this graph (measurement baseline): "pair", a
+        thread per (v, u) pair (parallelFine = 2), or "node", a thread per
+        node (parallelFine = 1)."""
         ms = C.c_double()
         bad = C.c_int64()
-        _check(self._L.h2h_fill_labels_plain(self.h, C.byref(ms), C.byref(bad)))
+        fn = {"pair": self._L.h2h_fill_labels_plain, "node": self._L.h2h_fill_labels_plain_node}[mapping]
+        _check(fn(self.h, C.byref(ms), C.byref(bad)))
         return ms.value, bad.value
 
     def save_index(self, path: str):

@@ -64,6 +64,12 @@ int h2h_query_batch_plain(const h2h_graph *g, const int *x_dev, const int *y_dev
  * L4 labels are exact whatever the order). */
 int h2h_fill_labels_plain(const h2h_graph *g, double *ms, int64_t *mismatches);
 
+/* The same with the reference's other GPU fill mapping (parallelFine = 1:
+ * one thread per node of a tree level walking its position list, one launch
+ * and one device synchronisation per level, L4 block enabled;
+ * makeH2HLabel_noCommunication_noHub / _D_noHub, kernel_functions.cu:802-888). */
+int h2h_fill_labels_plain_node(const h2h_graph *g, double *ms, int64_t *mismatches);
+
 /* Load generator for a query server (measurement tool).  Each request goes
  * to a uniformly drawn graph of graph_ids (vertex counts graph_n) with a
  * size drawn log-uniform in [size_lo, size_hi] pairs of uniform vertices.

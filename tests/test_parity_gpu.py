@@ -192,11 +192,12 @@ def test_tile_policies(cfg0_root, golden0, monkeypatch, policy):
     assert np.array_equal(_sha(g.labels()["dis"]), golden0["cfg0_C2_L4/sha256/dis"])
 
 
-def test_plain_fill_baseline_matches(cfg0_root):
-    """The reference's level-by-level fill mapping (the measurement baseline)
-    reproduces the dataflow fill's labels exactly."""
+@pytest.mark.parametrize("mapping", ["pair", "node"])
+def test_plain_fill_baseline_matches(cfg0_root, mapping):
+    """The reference's level-by-level fill mappings (the measurement
+    baselines) reproduce the dataflow fill's labels exactly."""
     import gpuh2h
     for C in (1, 2):
         g = build(gpuh2h.files_for(cfg0_root, "cfg0"), 6, C)
-        ms, bad = g.fill_labels_plain()
+        ms, bad = g.fill_labels_plain(mapping)
         assert bad == 0 and ms > 0
