@@ -24,7 +24,9 @@
 // (`ljunk`); later appends land after them, as in the reference.
 //
 // One thread-block cluster owns a cell (one CTA for the many small cells at
-// the bottom, up to 16 CTAs for the few large cells near the top).  Per
+// the bottom, up to 16 CTAs for the few large cells near the top; a step of
+// one cell -- the global order of a single graph -- runs instead as one
+// cooperative launch over all SMs, cell_grid_kernel further down).  Per
 // elimination the leader CTA takes the argmin and merges the eliminated
 // vertex's own list in shared memory; after a cluster barrier every warp of
 // every CTA rebuilds whole neighbour lists with a merge-path union of
