@@ -130,7 +130,7 @@ int h2h_batch_build(h2h_graph *const *graphs, int count, int threads, h2h_batch 
       for (auto &e : errs)
         if (e) std::rethrow_exception(e);
     };
-    per_graph([](gh::Graph &g) { gh::build_elimination_sets(g); });
+    gh::build_elimination_sets(b->gs);
     b->info.t_sets_us = clk.us();
     clk.reset();
     GH_CUDA(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));

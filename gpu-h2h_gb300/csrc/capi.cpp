@@ -124,7 +124,7 @@ int h2h_contract(h2h_graph *h, int use_gpu_contract) {
              "useGPUContract=0 selects the CPU partition contraction (partition_TD_T), which is not part of the "
              "GPU hot path");
     g.contract_device = use_gpu_contract;
-    gh::build_elimination_sets(g);
+    gh::build_elimination_sets({&g});
     gh::contract_gpu(g);  // with H == C no partition level runs (main.cu:96): the heap takes every vertex
     gh::build_tree_and_rmq(g);
     g.contracted = true;

@@ -845,24 +845,14 @@ T *dalloc(size_t n) {
 
 namespace {
 
-// Per-graph facts the launch plan needs: the level of every vertex, the
-// parallel-arc slack of every list, and where the global order starts.
+// Where a graph's global order starts: the vertices of the cells at levels
+// C..1 (the tail of elim).
 struct GraphLevels {
-  std::vector<int> level_of, dup;
   int heap_start = 0, heap_n = 0;
 };
 
 GraphLevels graph_levels(const Graph &g) {
   GraphLevels L;
-  const int n = g.n;
-  L.level_of.assign(n, 0);
-  for (int h = g.H; h >= 1; h--) {
-    const int64_t lo = (int64_t(1) << (h - 1)) - 1, hi = (int64_t(1) << h) - 2;
-    for (int64_t c = lo; c <= hi; c++)
-      for (int i = 0; i < g.cell_count[c]; i++) L.level_of[g.elim[g.cell_start[c] + i]] = h;
-  }
-  L.dup.assign(n, 0);  // filled by count_parallel_arcs
-  // global order: the vertices of cells at levels C..1 (tail of elim)
   int64_t heap_start = INT32_MAX;
   for (int h = g.C; h > 0; h--) {
     const int64_t lo = (int64_t(1) << (h - 1)) - 1, hi = (int64_t(1) << h) - 2;
@@ -870,43 +860,8 @@ GraphLevels graph_levels(const Graph &g) {
   }
   GH_CHECK(heap_start != INT32_MAX, H2H_ERR_ARG, "ChangeToGlobalHeight must be >= 1");
   L.heap_start = (int)heap_start;
-  L.heap_n = n - (int)heap_start;
+  L.heap_n = g.n - (int)heap_start;
   return L;
-}
-
-// Parallel-arc count of the vertices [b, e) (duplicate neighbour ids in the
-// input list), into L.dup.
-void count_parallel_arcs(const Graph &g, GraphLevels &L, int b, int e) {
-  std::vector<int> tmp;
-  for (int v = b; v < e; v++) {
-    const int lo = g.adj_off[v], hi = g.adj_off[v + 1];
-    bool sorted = true;
-    for (int i = lo + 1; i < hi && sorted; i++) sorted = g.adj_v[i - 1] < g.adj_v[i];
-    if (sorted) continue;  // strictly increasing: no parallel arcs
-    tmp.assign(g.adj_v.begin() + lo, g.adj_v.begin() + hi);
-    std::sort(tmp.begin(), tmp.end());
-    L.dup[v] = (int)(tmp.size() - (std::unique(tmp.begin(), tmp.end()) - tmp.begin()));
-  }
-}
-
-// Bound on a list of cell c while level h runs: alive cell members - 1 +
-// alive out-of-cell arcs (makeAdjcentNode's count) + parallel-arc slack.
-int cell_list_bound(const Graph &g, const GraphLevels &L, int64_t c, int h) {
-  int lmax = 1, alive = 0;
-  for (int i = g.cut_l[c]; i < g.cut_r[c]; i++) alive += L.level_of[g.part_ids[i]] <= h;
-  for (int i = g.cut_l[c]; i < g.cut_r[c]; i++) {
-    const int v = g.part_ids[i];
-    if (L.level_of[v] > h) continue;
-    int out = 0;
-    for (int e = g.adj_off[v]; e < g.adj_off[v + 1]; e++) {
-      const int u = g.adj_v[e];
-      if (L.level_of[u] > h) continue;
-      const int iu = g.id_hash[u];
-      if (iu < g.cut_l[c] || iu >= g.cut_r[c]) out++;
-    }
-    lmax = std::max(lmax, alive - 1 + out + L.dup[v]);
-  }
-  return lmax;
 }
 
 template <typename T>
@@ -922,53 +877,14 @@ ElimPlan::ElimPlan(const std::vector<Graph *> &graphs) : gs(graphs) {
   const int K = (int)gs.size();
   GH_CHECK(K >= 1, H2H_ERR_ARG, "no graph to contract");
   const bool force_global_stage = std::getenv("GPUH2H_GLOBAL_STAGING") != nullptr;
+  // cell list bounds come with the elimination sets (build_elimination_sets)
   std::vector<GraphLevels> L(K);
-  std::vector<std::vector<int>> bound(K);  // list bound per partition cell (levels > C)
   int threads = 1;
-  for (const Graph *g : gs) threads = std::max(threads, g->threads);
-  {
-    Pool pool(threads);
-    std::vector<std::exception_ptr> errs(K);
-    pool.parallel_for(K, 1, [&](int64_t lo, int64_t hi, int) {
-      for (int64_t i = lo; i < hi; i++) {
-        try {
-          L[i] = graph_levels(*gs[i]);
-          bound[i].assign(gs[i]->cell_start.size(), 1);
-        } catch (...) {
-          errs[i] = std::current_exception();
-        }
-      }
-    });
-    for (auto &e : errs)
-      if (e) std::rethrow_exception(e);
-    // parallel-arc counts, vertex chunks of every graph in parallel
-    struct VertexTask {
-      int i, b, e;
-    };
-    std::vector<VertexTask> vtasks;
-    for (int i = 0; i < K; i++)
-      for (int b = 0; b < gs[i]->n; b += 4096) vtasks.push_back({i, b, std::min(gs[i]->n, b + 4096)});
-    pool.parallel_for((int64_t)vtasks.size(), 1, [&](int64_t lo, int64_t hi, int) {
-      for (int64_t t = lo; t < hi; t++) count_parallel_arcs(*gs[vtasks[t].i], L[vtasks[t].i], vtasks[t].b, vtasks[t].e);
-    });
-    // list bounds of every partition cell of every graph, cells in parallel
-    struct CellTask {
-      int i, h;
-      int64_t c;
-    };
-    std::vector<CellTask> tasks;
-    for (int i = 0; i < K; i++)
-      for (int h = gs[i]->H; h > gs[i]->C; h--) {
-        const int64_t clo = (int64_t(1) << (h - 1)) - 1, chi = (int64_t(1) << h) - 2;
-        for (int64_t c = clo; c <= chi; c++) tasks.push_back({i, h, c});
-      }
-    pool.parallel_for((int64_t)tasks.size(), 8, [&](int64_t lo, int64_t hi, int) {
-      for (int64_t t = lo; t < hi; t++) {
-        const CellTask &T = tasks[t];
-        bound[T.i][T.c] = cell_list_bound(*gs[T.i], L[T.i], T.c, T.h);
-      }
-    });
+  for (const Graph *g : gs) {
+    threads = std::max(threads, g->threads);
+    GH_CHECK(g->cell_bound.size() == g->cell_start.size(), H2H_ERR_STATE, "elimination sets not built");
   }
+  for (int i = 0; i < K; i++) L[i] = graph_levels(*gs[i]);
   std::vector<int64_t> lbase(K);
   vbase.assign(K, 0);
   mbase.assign(K, 0);
@@ -1052,7 +968,7 @@ ElimPlan::ElimPlan(const std::vector<Graph *> &graphs) : gs(graphs) {
       level = h;
       const int64_t lo = (int64_t(1) << (h - 1)) - 1, hi = (int64_t(1) << h) - 2;
       for (int64_t c = lo; c <= hi; c++) {
-        const int cnt = g.cell_count[c], lb = bound[i][c];
+        const int cnt = g.cell_count[c], lb = g.cell_bound[c];
         cells.push_back({vbase[i] + g.cell_start[c], cnt, lb, size_class(std::max(cnt, lb))});
       }
     }

@@ -81,6 +81,8 @@ struct Graph {
   std::vector<int> cell_start, cell_count;  // NANHash first / NodeID per cell
   std::vector<int> elim;                    // nonAdjcentNode ids; rewritten to elimination order
   std::vector<int> cap;                     // placeOccupy (LUB capacity) per vertex
+  std::vector<int> cell_bound;              // per partition cell: bound on a list while its level runs
+  std::vector<int> dup;                     // parallel arcs per vertex (repeated neighbour ids)
   std::vector<int64_t> slot_off;            // LUB offset per vertex (partition-array layout)
   int64_t lub = 0;
   std::vector<double> layer_rate;           // afs[h] / n for the PartitionRate CSV
@@ -243,7 +245,9 @@ struct FillPlan {
 
 // Phases (one translation unit each).
 void load_graph(Graph &g, const std::string &edge, const std::string &idf, const std::string &cut);
-void build_elimination_sets(Graph &g);                 // elim_sets.cpp
+// elim_sets.cu: elimination sets, LUB capacities and layout, cell list
+// bounds and parallel-arc counts of one or more graphs, on the GPU
+void build_elimination_sets(const std::vector<Graph *> &gs);
 // contract.cu: partition levels H..C+1 and the global heap over levels <= C;
 // fills g.elim (elimination order) and g.x_off / x_id / x_w
 void contract_gpu(Graph &g);
