@@ -563,8 +563,31 @@ FillPlan::FillPlan(const std::vector<Graph *> &graphs, const TilePolicy &pol, co
   };
   const int K = (int)gs.size();
   GH_CHECK(K >= 1, H2H_ERR_ARG, "no graph to label");
+  int host_threads = 1;
+  for (const Graph *g : gs) host_threads = std::max(host_threads, g->threads);
+  host_threads = std::min(host_threads, K);
+  // per graph (in parallel): padded row total and widest separator
+  std::vector<int64_t> gdis(K, 0);
+  std::vector<int> gmax_m(K, 0);
+  {
+    Pool pool(host_threads);
+    pool.parallel_for(K, 1, [&](int64_t lo, int64_t hi, int) {
+      for (int64_t i = lo; i < hi; i++) {
+        const Graph &g = *gs[i];
+        int64_t d = 0;
+        int64_t mm = 0;
+        for (int v = 0; v < g.n; v++) {
+          d += (g.depth[v] + 3) & ~3;
+          mm = std::max<int64_t>(mm, g.x_off[v + 1] - g.x_off[v]);
+        }
+        gdis[i] = d;
+        gmax_m[i] = (int)mm;
+      }
+    });
+  }
   vbase.assign(K, 0);
   std::vector<int64_t> pbase(K, 0), dbase(K, 0);
+  int max_m = 0;
   for (int i = 0; i < K; i++) {
     const Graph &g = *gs[i];
     GH_CHECK((int64_t)N + g.n < INT32_MAX, H2H_ERR_ARG, "too many vertices in one batch");
@@ -573,16 +596,11 @@ FillPlan::FillPlan(const std::vector<Graph *> &graphs, const TilePolicy &pol, co
     dbase[i] = dis_total;
     N += g.n;
     pos_total += g.pos_hash[g.n];
-    for (int v = 0; v < g.n; v++) dis_total += (g.depth[v] + 3) & ~3;
+    dis_total += gdis[i];
+    max_m = std::max(max_m, gmax_m[i]);
   }
-  int host_threads = 1;
-  for (const Graph *g : gs) host_threads = std::max(host_threads, g->threads);
-  host_threads = std::min(host_threads, K);
   std::vector<int64_t> f_drow(N + 1, 0), f_pos_hash(N + 1, 0);
   std::vector<int> f_father(N), f_depth(N), f_hld(N);
-  int max_m = 0;
-  for (const Graph *g : gs)
-    for (int v = 0; v < g->n; v++) max_m = std::max<int64_t>(max_m, g->x_off[v + 1] - g->x_off[v]);
   std::vector<int64_t> sbase(K, 0);
   int64_t seg_total = 0;
   for (int i = 0; i < K; i++) {
@@ -688,17 +706,37 @@ void FillPlan::release_work() {
 }
 
 std::vector<int> FillPlan::level_classes() const {
-  int nlev = 0;
-  for (const Graph *g : gs) nlev = std::max(nlev, (int)g->tree_hash.size() - 1);
+  const int K = (int)gs.size();
+  int nlev = 0, host_threads = 1;
+  for (const Graph *g : gs) {
+    nlev = std::max(nlev, (int)g->tree_hash.size() - 1);
+    host_threads = std::max(host_threads, g->threads);
+  }
+  // per graph (in parallel), then summed: nodes and min-plus updates per level
+  std::vector<std::vector<int64_t>> gwork(K);
+  {
+    Pool pool(std::min(host_threads, K));
+    pool.parallel_for(K, 1, [&](int64_t lo, int64_t hi, int) {
+      for (int64_t i = lo; i < hi; i++) {
+        const Graph *g = gs[i];
+        std::vector<int64_t> &w = gwork[i];
+        w.assign(std::max(0, (int)g->tree_hash.size() - 1), 0);
+        for (int l = 0; l + 1 < (int)g->tree_hash.size(); l++)
+          for (int q = g->tree_hash[l]; q < g->tree_hash[l + 1]; q++) {
+            const int v = g->tree_bfs[q];
+            w[l] += (g->pos_hash[v + 1] - g->pos_hash[v] - 1) * (int64_t)g->depth[v];
+          }
+      }
+    });
+  }
   std::vector<int64_t> width(nlev, 0), work(nlev, 0);
-  for (const Graph *g : gs)
+  for (int i = 0; i < K; i++) {
+    const Graph *g = gs[i];
     for (int l = 0; l + 1 < (int)g->tree_hash.size(); l++) {
       width[l] += g->tree_hash[l + 1] - g->tree_hash[l];
-      for (int q = g->tree_hash[l]; q < g->tree_hash[l + 1]; q++) {
-        const int v = g->tree_bfs[q];
-        work[l] += (g->pos_hash[v + 1] - g->pos_hash[v] - 1) * (int64_t)g->depth[v];
-      }
+      work[l] += gwork[i][l];
     }
+  }
   // narrow: fewer nodes than SMs, whatever their work (the critical path);
   // heavy: a wider level whose nodes average at least 2^18 min-plus updates
   // (GPUH2H_HEAVY_LEVEL_WORK overrides the figure)
