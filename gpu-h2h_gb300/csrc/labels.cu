@@ -409,6 +409,25 @@ __global__ void count_mismatch_kernel(const int *a, const int *b, int64_t n, uns
   if (c) atomicAdd(bad, c);
 }
 
+// Chunk k's first ticket, from per-level rows (first chunk, first ticket,
+// step): the level holding k by binary search, then an arithmetic step;
+// entry nchunks closes the table.
+__global__ void chunk_table_kernel(const int64_t *ltab, int nlev, int64_t nchunks, int64_t ntiles, int *chunks) {
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k <= nchunks;
+       k += (int64_t)gridDim.x * blockDim.x) {
+    if (k == nchunks) {
+      chunks[k] = (int)ntiles;
+      continue;
+    }
+    int lo = 0, hi = nlev - 1;  // last level whose first chunk is <= k
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (ltab[3 * mid] <= k) lo = mid; else hi = mid - 1;
+    }
+    chunks[k] = (int)(ltab[3 * lo + 1] + (k - ltab[3 * lo]) * ltab[3 * lo + 2]);
+  }
+}
+
 // tile_node[t] = v for the tickets of every node v.  One warp per node.
 __global__ void expand_tiles_kernel(const int *node_first, const int *node_ntiles, int *tile_node, int n) {
   const int lane = threadIdx.x & 31;
@@ -565,25 +584,36 @@ FillPlan::FillPlan(const std::vector<Graph *> &graphs, const TilePolicy &pol, co
   GH_CHECK(K >= 1, H2H_ERR_ARG, "no graph to label");
   int host_threads = 1;
   for (const Graph *g : gs) host_threads = std::max(host_threads, g->threads);
-  host_threads = std::min(host_threads, K);
-  // per graph (in parallel): padded row total and widest separator
+  // vertex ranges of every graph, in parallel: padded row totals and the
+  // widest separator
+  struct VRange {
+    int g, v0, v1;
+  };
+  std::vector<VRange> vr;
+  for (int i = 0; i < K; i++)
+    for (int v = 0; v < gs[i]->n; v += 65536) vr.push_back({i, v, std::min(gs[i]->n, v + 65536)});
+  const int64_t nvr = (int64_t)vr.size();
+  std::vector<int64_t> rdis(nvr, 0), rbase(nvr, 0);
+  std::vector<int> rmax_m(nvr, 0);
+  Pool pool(host_threads);
+  pool.parallel_for(nvr, 1, [&](int64_t lo, int64_t hi, int) {
+    for (int64_t r = lo; r < hi; r++) {
+      const Graph &g = *gs[vr[r].g];
+      int64_t d = 0, mm = 0;
+      for (int v = vr[r].v0; v < vr[r].v1; v++) {
+        d += (g.depth[v] + 3) & ~3;
+        mm = std::max<int64_t>(mm, g.x_off[v + 1] - g.x_off[v]);
+      }
+      rdis[r] = d;
+      rmax_m[r] = (int)mm;
+    }
+  });
   std::vector<int64_t> gdis(K, 0);
   std::vector<int> gmax_m(K, 0);
-  {
-    Pool pool(host_threads);
-    pool.parallel_for(K, 1, [&](int64_t lo, int64_t hi, int) {
-      for (int64_t i = lo; i < hi; i++) {
-        const Graph &g = *gs[i];
-        int64_t d = 0;
-        int64_t mm = 0;
-        for (int v = 0; v < g.n; v++) {
-          d += (g.depth[v] + 3) & ~3;
-          mm = std::max<int64_t>(mm, g.x_off[v + 1] - g.x_off[v]);
-        }
-        gdis[i] = d;
-        gmax_m[i] = (int)mm;
-      }
-    });
+  for (int64_t r = 0; r < nvr; r++) {
+    rbase[r] = gdis[vr[r].g];  // offset inside the graph's rows
+    gdis[vr[r].g] += rdis[r];
+    gmax_m[vr[r].g] = std::max(gmax_m[vr[r].g], rmax_m[r]);
   }
   vbase.assign(K, 0);
   std::vector<int64_t> pbase(K, 0), dbase(K, 0);
@@ -610,29 +640,27 @@ FillPlan::FillPlan(const std::vector<Graph *> &graphs, const TilePolicy &pol, co
   }
   std::vector<int64_t> f_seg_off(N + 1, 0);
   std::vector<int> f_htop(N), f_hpos(N);
-  {
-    Pool pool(host_threads);
-    pool.parallel_for(K, 1, [&](int64_t lo, int64_t hi, int) {
-      for (int64_t i = lo; i < hi; i++) {
-        const Graph &g = *gs[i];
-        const int vb = vbase[i];
-        const int64_t pb = pbase[i];
-        int64_t d = dbase[i];
-        for (int v = 0; v < g.n; v++) {
-          const int V = vb + v;
-          f_drow[V] = d;
-          d += (g.depth[v] + 3) & ~3;
-          f_pos_hash[V] = pb + g.pos_hash[v];
-          f_father[V] = g.father[v] < 0 ? -1 : g.father[v] + vb;
-          f_depth[V] = g.depth[v];
-          f_hld[V] = g.hld[v] + vb;
-          f_htop[V] = g.htop[v] + vb;
-          f_hpos[V] = g.hpos[v] + vb;
-          f_seg_off[V] = sbase[i] + g.seg_off[v];
-        }
+  pool.parallel_for(nvr, 1, [&](int64_t lo, int64_t hi, int) {
+    for (int64_t r = lo; r < hi; r++) {
+      const int i = vr[r].g;
+      const Graph &g = *gs[i];
+      const int vb = vbase[i];
+      const int64_t pb = pbase[i];
+      int64_t d = dbase[i] + rbase[r];
+      for (int v = vr[r].v0; v < vr[r].v1; v++) {
+        const int V = vb + v;
+        f_drow[V] = d;
+        d += (g.depth[v] + 3) & ~3;
+        f_pos_hash[V] = pb + g.pos_hash[v];
+        f_father[V] = g.father[v] < 0 ? -1 : g.father[v] + vb;
+        f_depth[V] = g.depth[v];
+        f_hld[V] = g.hld[v] + vb;
+        f_htop[V] = g.htop[v] + vb;
+        f_hpos[V] = g.hpos[v] + vb;
+        f_seg_off[V] = sbase[i] + g.seg_off[v];
       }
-    });
-  }
+    }
+  });
   f_drow[N] = dis_total;
   f_pos_hash[N] = pos_total;
   f_seg_off[N] = seg_total;
@@ -705,37 +733,55 @@ void FillPlan::release_work() {
   seg_off = nullptr;
 }
 
-std::vector<int> FillPlan::level_classes() const {
-  const int K = (int)gs.size();
-  int nlev = 0, host_threads = 1;
-  for (const Graph *g : gs) {
-    nlev = std::max(nlev, (int)g->tree_hash.size() - 1);
-    host_threads = std::max(host_threads, g->threads);
+// Work items of the host passes over the forest: (graph, level, BFS range
+// of at most kItemNodes nodes), graph by graph, levels in order.
+namespace {
+constexpr int kItemNodes = 32768;
+struct LevelItem {
+  int g, l, q0, q1;
+};
+std::vector<LevelItem> level_items(const std::vector<Graph *> &gs) {
+  std::vector<LevelItem> items;
+  for (int i = 0; i < (int)gs.size(); i++) {
+    const Graph &g = *gs[i];
+    for (int l = 0; l + 1 < (int)g.tree_hash.size(); l++)
+      for (int q = g.tree_hash[l]; q < g.tree_hash[l + 1]; q += kItemNodes)
+        items.push_back({i, l, q, std::min(q + kItemNodes, g.tree_hash[l + 1])});
   }
-  // per graph (in parallel), then summed: nodes and min-plus updates per level
-  std::vector<std::vector<int64_t>> gwork(K);
+  return items;
+}
+int host_threads_of(const std::vector<Graph *> &gs) {
+  int t = 1;
+  for (const Graph *g : gs) t = std::max(t, g->threads);
+  return t;
+}
+}  // namespace
+
+std::vector<int> FillPlan::level_classes() const {
+  int nlev = 0;
+  for (const Graph *g : gs) nlev = std::max(nlev, (int)g->tree_hash.size() - 1);
+  // nodes and min-plus updates per forest level, summed over items computed in parallel
+  const std::vector<LevelItem> items = level_items(gs);
+  std::vector<int64_t> iwork(items.size(), 0);
   {
-    Pool pool(std::min(host_threads, K));
-    pool.parallel_for(K, 1, [&](int64_t lo, int64_t hi, int) {
-      for (int64_t i = lo; i < hi; i++) {
-        const Graph *g = gs[i];
-        std::vector<int64_t> &w = gwork[i];
-        w.assign(std::max(0, (int)g->tree_hash.size() - 1), 0);
-        for (int l = 0; l + 1 < (int)g->tree_hash.size(); l++)
-          for (int q = g->tree_hash[l]; q < g->tree_hash[l + 1]; q++) {
-            const int v = g->tree_bfs[q];
-            w[l] += (g->pos_hash[v + 1] - g->pos_hash[v] - 1) * (int64_t)g->depth[v];
-          }
+    Pool pool(host_threads_of(gs));
+    pool.parallel_for((int64_t)items.size(), 1, [&](int64_t lo, int64_t hi, int) {
+      for (int64_t t = lo; t < hi; t++) {
+        const LevelItem &it = items[t];
+        const Graph &g = *gs[it.g];
+        int64_t w = 0;
+        for (int q = it.q0; q < it.q1; q++) {
+          const int v = g.tree_bfs[q];
+          w += (g.pos_hash[v + 1] - g.pos_hash[v] - 1) * (int64_t)g.depth[v];
+        }
+        iwork[t] = w;
       }
     });
   }
   std::vector<int64_t> width(nlev, 0), work(nlev, 0);
-  for (int i = 0; i < K; i++) {
-    const Graph *g = gs[i];
-    for (int l = 0; l + 1 < (int)g->tree_hash.size(); l++) {
-      width[l] += g->tree_hash[l + 1] - g->tree_hash[l];
-      work[l] += gwork[i][l];
-    }
+  for (size_t t = 0; t < items.size(); t++) {
+    width[items[t].l] += items[t].q1 - items[t].q0;
+    work[items[t].l] += iwork[t];
   }
   // narrow: fewer nodes than SMs, whatever their work (the critical path);
   // heavy: a wider level whose nodes average at least 2^18 min-plus updates
@@ -781,31 +827,45 @@ void FillPlan::build_tiles(const TilePolicy &pol) {
     nt_node = ((d + cb - 1) / cb) * ((std::max(m, 1) + sc - 1) / sc);
     return false;
   };
-  int host_threads = 1;
-  for (const Graph *g : gs) host_threads = std::max(host_threads, g->threads);
-  Pool pool(std::min(host_threads, K));
-  // pass 1: tiles per (level, graph), staging bounds per graph
-  std::vector<std::vector<int64_t>> cnt(K);
-  std::vector<int> mu(K, 1), mc(K, 1);
-  pool.parallel_for(K, 1, [&](int64_t lo, int64_t hi, int) {
-    for (int64_t i = lo; i < hi; i++) {
-      const Graph &g = *gs[i];
-      const int gl = (int)g.tree_hash.size() - 1;
-      cnt[i].assign(gl, 0);
-      for (int l = 0; l < gl; l++) {
-        const int wb = lcls[l];
-        for (int q = g.tree_hash[l]; q < g.tree_hash[l + 1]; q++) {
-          const int v = g.tree_bfs[q], d = g.depth[v];
-          const int m = (int)(g.pos_hash[v + 1] - g.pos_hash[v]) - 1;
-          int nt_node, cb, sc;
-          const bool one = tiles_of(wb, m, d, nt_node, cb, sc);
-          cnt[i][l] += nt_node;
-          mu[i] = std::max(mu[i], one ? m : std::min(m, sc));
-          mc[i] = std::max(mc[i], one ? d : std::min(d, cb));
-        }
+  Pool pool(host_threads_of(gs));
+  // pass 1 (items in parallel): every node's tile count and shape, tiles
+  // per item, staging bounds
+  const std::vector<LevelItem> items = level_items(gs);
+  const int64_t nitems = (int64_t)items.size();
+  std::vector<int> host((size_t)4 * N);
+  int *nfirst = host.data(), *nt = nfirst + N, *ncb = nfirst + 2 * N, *nsc = nfirst + 3 * N;
+  std::vector<int64_t> icnt(nitems, 0);
+  std::vector<int> imu(nitems, 1), imc(nitems, 1);
+  pool.parallel_for(nitems, 1, [&](int64_t lo, int64_t hi, int) {
+    for (int64_t t = lo; t < hi; t++) {
+      const LevelItem &it = items[t];
+      const Graph &g = *gs[it.g];
+      const int vb = vbase[it.g], wb = lcls[it.l];
+      int64_t c = 0;
+      int mu = 1, mc = 1;
+      for (int q = it.q0; q < it.q1; q++) {
+        const int v = g.tree_bfs[q], V = vb + v, d = g.depth[v];
+        const int m = (int)(g.pos_hash[v + 1] - g.pos_hash[v]) - 1;
+        int nt_node, cb, sc;
+        const bool one = tiles_of(wb, m, d, nt_node, cb, sc);
+        nt[V] = nt_node;
+        ncb[V] = cb;
+        nsc[V] = sc;
+        c += nt_node;
+        mu = std::max(mu, one ? m : std::min(m, sc));
+        mc = std::max(mc, one ? d : std::min(d, cb));
       }
+      icnt[t] = c;
+      imu[t] = mu;
+      imc[t] = mc;
     }
   });
+  // tickets: forest level by forest level, graphs in order inside a level,
+  // BFS order inside a graph's level; the items of a (graph, level) are
+  // consecutive in BFS order
+  std::vector<std::vector<int64_t>> cnt(K);
+  for (int i = 0; i < K; i++) cnt[i].assign(std::max(0, (int)gs[i]->tree_hash.size() - 1), 0);
+  for (int64_t t = 0; t < nitems; t++) cnt[items[t].g][items[t].l] += icnt[t];
   std::vector<std::vector<int64_t>> off(K);
   int64_t total = 0;
   for (int i = 0; i < K; i++) off[i].assign(cnt[i].size(), 0);
@@ -817,32 +877,26 @@ void FillPlan::build_tiles(const TilePolicy &pol) {
       }
   ntiles = total;
   GH_CHECK(ntiles < INT32_MAX, H2H_ERR_ARG, "too many fill tiles");
-  max_u = *std::max_element(mu.begin(), mu.end());
-  max_c = *std::max_element(mc.begin(), mc.end());
+  max_u = *std::max_element(imu.begin(), imu.end());
+  max_c = *std::max_element(imc.begin(), imc.end());
+  std::vector<int64_t> ibase(nitems, 0);
+  for (int64_t t = 0; t < nitems; t++) {
+    const bool first = t == 0 || items[t - 1].g != items[t].g || items[t - 1].l != items[t].l;
+    ibase[t] = first ? off[items[t].g][items[t].l] : ibase[t - 1] + icnt[t - 1];
+  }
   mark("pass 1");
-  // pass 2: per node its first ticket, tile count and tile shape; the
-  // ticket -> node array is expanded on the device
-  std::vector<int> host((size_t)4 * N);
-  int *nfirst = host.data(), *nt = nfirst + N, *ncb = nfirst + 2 * N, *nsc = nfirst + 3 * N;
-  pool.parallel_for(K, 1, [&](int64_t lo, int64_t hi, int) {
-    for (int64_t i = lo; i < hi; i++) {
-      const Graph &g = *gs[i];
-      const int vb = vbase[i];
-      const int gl = (int)g.tree_hash.size() - 1;
-      for (int l = 0; l < gl; l++) {
-        const int wb = lcls[l];
-        int64_t t = off[i][l];
-        for (int q = g.tree_hash[l]; q < g.tree_hash[l + 1]; q++) {
-          const int v = g.tree_bfs[q], V = vb + v, d = g.depth[v];
-          const int m = (int)(g.pos_hash[v + 1] - g.pos_hash[v]) - 1;
-          int nt_node, cb, sc;
-          tiles_of(wb, m, d, nt_node, cb, sc);
-          nfirst[V] = (int)t;
-          nt[V] = nt_node;
-          ncb[V] = cb;
-          nsc[V] = sc;
-          t += nt_node;
-        }
+  // pass 2 (items in parallel): every node's first ticket; the ticket ->
+  // node array is expanded on the device
+  pool.parallel_for(nitems, 1, [&](int64_t lo, int64_t hi, int) {
+    for (int64_t t = lo; t < hi; t++) {
+      const LevelItem &it = items[t];
+      const Graph &g = *gs[it.g];
+      const int vb = vbase[it.g];
+      int64_t tk = ibase[t];
+      for (int q = it.q0; q < it.q1; q++) {
+        const int V = vb + g.tree_bfs[q];
+        nfirst[V] = (int)tk;
+        tk += nt[V];
       }
     }
   });
@@ -859,7 +913,9 @@ void FillPlan::build_tiles(const TilePolicy &pol) {
   // tiles than resident warps hands them out in groups (fewer atomics on the
   // counter); any other level one by one, so its tiles spread over warps.
   // When every level goes one by one there is no table (chunk k = tile k).
-  std::vector<int> chunks;
+  // the table is built on the device from one (first chunk, first ticket,
+  // step) row per level
+  std::vector<int64_t> ltab;  // per level: first chunk, first ticket, step
   {
     const int64_t warps = (int64_t)nsm * 64;
     std::vector<int64_t> lt(nlev, 0);
@@ -875,22 +931,33 @@ void FillPlan::build_tiles(const TilePolicy &pol) {
     }
     nchunks = grouped ? nc : ntiles;
     if (grouped) {
-      chunks.resize((size_t)nc + 1);
+      ltab.resize(3 * (size_t)nlev);
       int64_t t = 0, k = 0;
       for (int l = 0; l < nlev; l++) {
-        const int64_t e = t + lt[l];  // this level's tickets are [t, e)
-        for (int64_t c = t; c < e; c += step[l]) chunks[k++] = (int)c;
-        t = e;
+        ltab[3 * l] = k;
+        ltab[3 * l + 1] = t;
+        ltab[3 * l + 2] = step[l];
+        k += (lt[l] + step[l] - 1) / step[l];
+        t += lt[l];
       }
       GH_CHECK(t == ntiles && k == nc, H2H_ERR_STATE, "fill chunks do not cover the tiles");
-      chunks[nc] = (int)ntiles;
     }
   }
   mark("chunks");
   GH_CUDA(cudaMemcpy(tiles + ntiles, host.data(), sizeof(int) * 4 * (int64_t)N, cudaMemcpyHostToDevice));
-  if (!chunks.empty())
-    GH_CUDA(cudaMemcpy(tiles + ntiles + 4 * (int64_t)N, chunks.data(), sizeof(int) * chunks.size(),
-                       cudaMemcpyHostToDevice));
+  if (!ltab.empty()) {
+    int64_t *d_ltab = nullptr;
+    GH_CUDA(cudaMalloc(&d_ltab, sizeof(int64_t) * ltab.size()));
+    cudaError_t e = cudaMemcpy(d_ltab, ltab.data(), sizeof(int64_t) * ltab.size(), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+      chunk_table_kernel<<<std::max(1, std::min<int>(nsm * 8, (int)((nchunks + 255) / 256))), 256>>>(
+          d_ltab, nlev, nchunks, ntiles, tiles + ntiles + 4 * (int64_t)N);
+      e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    cudaFree(d_ltab);
+    GH_CUDA(e);
+  }
   expand_tiles_kernel<<<std::max(1, std::min(8192, (N * 32 + 255) / 256)), 256>>>(tiles + ntiles, tiles + ntiles + N,
                                                                                   tiles, N);
   GH_CUDA(cudaGetLastError());
