@@ -452,7 +452,7 @@ __global__ void __launch_bounds__(512) elim_kernel(ElimArgs A) {
 // eliminations whose neighbour merges want more SMs than that.
 //
 // Ownership: block r of a cell's nb blocks owns the vertices u with
-// u mod nb == r.  It keeps the keys of the candidates it owns in shared
+// owner_of(u, nb) == r (a scrambled id mod nb).  It keeps the keys of the candidates it owns in shared
 // memory (their slots in cpos), merges the lists of the neighbours it owns
 // (candidates or not), refreshes their keys and retires its picked
 // candidate.  So a block finds its share of v's neighbours without a memory
@@ -498,6 +498,20 @@ __device__ __forceinline__ void block_best(int &bs, int &bd, int &bi, int &bp, i
   __syncthreads();
   if (threadIdx.x == 0)
     for (int w = 1; w < nw; w++) better(bs, bd, bi, bp, rs[w], rd[w], ri[w], rp[w]);
+}
+
+// The block of a cell's nb blocks that owns vertex u.  Ids are scrambled
+// first (the murmur3 finaliser): separator vertices of a grid-like graph are
+// often evenly spaced ids, and a plain u mod nb would pile them onto a few
+// blocks.
+__host__ __device__ __forceinline__ int owner_of(int u, int nb) {
+  unsigned x = (unsigned)u;
+  x ^= x >> 16;
+  x *= 0x85ebca6bu;
+  x ^= x >> 13;
+  x *= 0xc2b2ae35u;
+  x ^= x >> 16;
+  return (int)(x % (unsigned)nb);
 }
 
 __device__ __forceinline__ unsigned ld_acquire_u32(const unsigned *p) {
@@ -571,7 +585,7 @@ __global__ void __launch_bounds__(512, 1) cell_grid_kernel(GridArgs H) {
   __syncthreads();
   for (int i = tid; i < k; i += nthr) {
     const int v = A.elim[start + i];
-    if (v % nb == r) {
+    if (owner_of(v, nb) == r) {
       const int t = atomicAdd(&s_nslot, 1);
       if (t < H.slice_max) {
         cid[t] = v;
@@ -622,7 +636,7 @@ __global__ void __launch_bounds__(512, 1) cell_grid_kernel(GridArgs H) {
           s_bc[0] = bi;
           s_bc[1] = bs - bd;
           if (r == 0) A.elim[start + j] = bi;
-          if (bi % nb == r) {  // the owner retires the candidate
+          if (owner_of(bi, nb) == r) {  // the owner retires the candidate
             dead[bp] = 1;
             A.cpos[bi] = -1;
           }
@@ -681,7 +695,7 @@ __global__ void __launch_bounds__(512, 1) cell_grid_kernel(GridArgs H) {
     const int c = s_bc[2];
     // ---- the neighbours this block owns
     for (int i = tid; i < c; i += nthr)
-      if (aid[i] % nb == r) mine[atomicAdd(&s_nmine, 1)] = i;
+      if (owner_of(aid[i], nb) == r) mine[atomicAdd(&s_nmine, 1)] = i;
     __syncthreads();
     const int nm = s_nmine;
     for (int t = wid; t < nm; t += nw) {
@@ -989,21 +1003,22 @@ ElimPlan::ElimPlan(const std::vector<Graph *> &graphs) : gs(graphs) {
   auto al = [](int64_t bb) { return (bb + 15) & ~int64_t(15); };
   int64_t pstage_ints = 0, partial_max = 0;
   std::vector<int> gmap;
-  // Whole-step cooperative launch: one block per SM.  Taken by default for a
-  // step of one cell -- the global order of a single graph, one long chain
-  // that the cluster kernel would give 16 SMs (1.5x faster on road graphs).
-  // Measured on road graphs, steps of several cells run faster on clusters:
-  // at 1 block of 4-16 warps per SM the cooperative kernel has fewer merge
-  // warps per cell than the cluster kernel's several CTAs per SM, and its
-  // barrier goes through L2.  GPUH2H_GRID_CELLS (most cells a cooperative
-  // launch takes) overrides.  Blocks go to cells greedily by an estimate of
-  // the chain time, eliminations x (1 + merge rounds x list length), merge
-  // rounds ~ 2 x list bound / warps.
+  // Whole-step cooperative launch: one block per SM.  Taken when it gives a
+  // cell at least 3x the merge warps a 16-CTA cluster would: the global
+  // order of a single graph (one long chain; 1.5x faster on road graphs) and
+  // the few top cells whose long lists leave a cluster CTA room for only 4
+  // warps (3.6M-vertex road graph, level 3: 923 -> 470 ms).  At smaller
+  // ratios the cluster kernel wins, by up to 2.7x on a level of 8 cells:
+  // ncu shows the same work and instructions, but the cooperative blocks
+  // wait at the cell barrier for the slowest block of the cell.
+  // GPUH2H_GRID_CELLS (most cells a cooperative launch takes) overrides the
+  // rule.  Blocks go to cells greedily by an estimate of the chain time,
+  // eliminations x (1 + merge rounds x list length), merge rounds ~ 2 x list
+  // bound / warps.
   auto grid_launch = [&](const std::vector<Cell> &cells, int st, bool heap) -> bool {
     const int ncell = (int)cells.size();
-    int max_cells = 1;
-    if (const char *e = std::getenv("GPUH2H_GRID_CELLS")) max_cells = std::atoi(e);
-    if (force_cluster || ncell > max_cells || ncell > nsm) return false;
+    const char *env_cells = std::getenv("GPUH2H_GRID_CELLS");
+    if (force_cluster || ncell > nsm || (env_cells && ncell > std::atoi(env_cells))) return false;
     int lmax = 1, kmax = 1;
     for (const Cell &c : cells) {
       lmax = std::max(lmax, c.lbound);
@@ -1026,13 +1041,13 @@ ElimPlan::ElimPlan(const std::vector<Graph *> &graphs) : gs(graphs) {
       used++;
       pq.push({est(c, nb[c]), c});
     }
-    // candidate slots: block r of cell c owns the cell's vertices v with v mod nb == r
+    // candidate slots: block r of cell c owns the cell's vertices v with owner_of(v, nb) == r
     int slice_max = 1;
     {
       std::vector<int> cnt;
       for (int c = 0; c < ncell; c++) {
         cnt.assign(nb[c], 0);
-        for (int i = 0; i < cells[c].count; i++) cnt[f_elim[cells[c].start + i] % nb[c]]++;
+        for (int i = 0; i < cells[c].count; i++) cnt[owner_of(f_elim[cells[c].start + i], nb[c])]++;
         for (int x : cnt) slice_max = std::max(slice_max, x);
       }
       int64_t arrivals = 0;
@@ -1053,6 +1068,16 @@ ElimPlan::ElimPlan(const std::vector<Graph *> &graphs) : gs(graphs) {
         per < 1) {
       cudaGetLastError();
       return false;
+    }
+    if (!env_cells) {
+      // merge warps per cell: a cluster of 16 CTAs with as many warps as
+      // their merge buffers leave room for (the group loop's rule, for the
+      // step's largest cell) against nsm / ncell blocks of hw warps
+      const int64_t own_c = 3 * al(4LL * kmax) + 2 * al(4LL * lmax);
+      int nwc = 16;
+      while (nwc > 4 && own_c + 2 * al(4LL * lmax * nwc) > smem_dyn) nwc >>= 1;
+      const double grid_warps = (double)nsm / ncell * hw, cluster_warps = 16.0 * nwc;
+      if (grid_warps < 3.0 * cluster_warps) return false;
     }
     Launch Lc;
     Lc.step = st;
