@@ -1003,22 +1003,22 @@ ElimPlan::ElimPlan(const std::vector<Graph *> &graphs) : gs(graphs) {
   auto al = [](int64_t bb) { return (bb + 15) & ~int64_t(15); };
   int64_t pstage_ints = 0, partial_max = 0;
   std::vector<int> gmap;
-  // Whole-step cooperative launch: one block per SM.  Taken when it gives a
-  // cell at least 3x the merge warps a 16-CTA cluster would: the global
-  // order of a single graph (one long chain; 1.5x faster on road graphs) and
-  // the few top cells whose long lists leave a cluster CTA room for only 4
-  // warps (3.6M-vertex road graph, level 3: 923 -> 470 ms).  At smaller
-  // ratios the cluster kernel wins, by up to 2.7x on a level of 8 cells:
-  // ncu shows the same work and instructions, but the cooperative blocks
-  // wait at the cell barrier for the slowest block of the cell.
-  // GPUH2H_GRID_CELLS (most cells a cooperative launch takes) overrides the
-  // rule.  Blocks go to cells greedily by an estimate of the chain time,
-  // eliminations x (1 + merge rounds x list length), merge rounds ~ 2 x list
-  // bound / warps.
+  // Whole-step cooperative launch: one block per SM, for steps of at most
+  // nsm / 2 cells (GPUH2H_GRID_CELLS overrides), where a cell gets two SMs
+  // or more -- the cluster kernel caps a cell at 16 CTAs, and long lists
+  // leave its CTAs room for only a few warps.  Measured on road graphs
+  // against clusters: a single graph's global order 54 -> 33 ms (264k
+  // vertices); the 3.6M-vertex graph's partition levels 1.78 -> 1.21 s
+  // (level 3, 4 cells: 923 -> 474 ms; level 5, 16 cells: 379 -> 285 ms); a
+  // 64-graph batch's partition steps 132 -> 123 ms and global orders 49 ->
+  // 42 ms; steps of more cells than that ran slower.  Blocks go to cells
+  // greedily by an estimate of the chain time, eliminations x (1 + merge
+  // rounds x list length), merge rounds ~ 2 x list bound / warps.
   auto grid_launch = [&](const std::vector<Cell> &cells, int st, bool heap) -> bool {
     const int ncell = (int)cells.size();
-    const char *env_cells = std::getenv("GPUH2H_GRID_CELLS");
-    if (force_cluster || ncell > nsm || (env_cells && ncell > std::atoi(env_cells))) return false;
+    int max_cells = std::max(1, nsm / 2);
+    if (const char *e = std::getenv("GPUH2H_GRID_CELLS")) max_cells = std::atoi(e);
+    if (force_cluster || ncell > nsm || ncell > max_cells) return false;
     int lmax = 1, kmax = 1;
     for (const Cell &c : cells) {
       lmax = std::max(lmax, c.lbound);
@@ -1068,16 +1068,6 @@ ElimPlan::ElimPlan(const std::vector<Graph *> &graphs) : gs(graphs) {
         per < 1) {
       cudaGetLastError();
       return false;
-    }
-    if (!env_cells) {
-      // merge warps per cell: a cluster of 16 CTAs with as many warps as
-      // their merge buffers leave room for (the group loop's rule, for the
-      // step's largest cell) against nsm / ncell blocks of hw warps
-      const int64_t own_c = 3 * al(4LL * kmax) + 2 * al(4LL * lmax);
-      int nwc = 16;
-      while (nwc > 4 && own_c + 2 * al(4LL * lmax * nwc) > smem_dyn) nwc >>= 1;
-      const double grid_warps = (double)nsm / ncell * hw, cluster_warps = 16.0 * nwc;
-      if (grid_warps < 3.0 * cluster_warps) return false;
     }
     Launch Lc;
     Lc.step = st;
