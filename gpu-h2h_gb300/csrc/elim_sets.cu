@@ -26,12 +26,8 @@
 // from the levels below) gives every chunk and cell its offset; each chunk
 // writes its interior vertices in position order and retires them.
 #include <algorithm>
-#include <climits>
-#include <cstdio>
-#include <cstdlib>
 
 #include "graph.h"
-#include "pool.h"
 
 namespace gh {
 
