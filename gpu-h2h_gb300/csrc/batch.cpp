@@ -175,7 +175,9 @@ int h2h_batch_build(h2h_graph *const *graphs, int count, int threads, h2h_batch 
                    (long long)b->info.t_tree_us, sum, mx);
     }
     clk.reset();
-    gh::TilePolicy pol;
+    int height = 0;
+    for (const gh::Graph *g : b->gs) height = std::max(height, g->tree_height);
+    gh::TilePolicy pol = gh::TilePolicy::for_height(height);
     if (const char *e = std::getenv("GPUH2H_TILE_POLICY"))
       GH_CHECK(pol.parse(e), H2H_ERR_ARG, "GPUH2H_TILE_POLICY: expected 12 entries small_work/col_block/sep_chunk");
     b->fill = std::make_unique<gh::FillPlan>(b->gs, pol, b->elim->lists);
@@ -186,6 +188,7 @@ int h2h_batch_build(h2h_graph *const *graphs, int count, int threads, h2h_batch 
     b->fill->enqueue(b->stream, fev);
     b->fill->check_error();
     b->info.t_fill_us = event_us(b->ev[0], b->ev[3]);
+    b->fill->trace_report();
     clk.reset();
     b->fill->attach(true);
     for (gh::Graph *g : b->gs) {
@@ -219,7 +222,8 @@ int h2h_batch_rebuild(h2h_batch *b) {
       try {
         b->elim->enqueue(b->stream);
         b->elim->enqueue_gather(b->stream);
-        b->fill->enqueue(b->stream, nullptr);
+        cudaEvent_t fev[2] = {b->ev[1], b->ev[2]};  // recorded by the graph around the fill kernel
+        b->fill->enqueue(b->stream, fev);
       } catch (...) {
         cudaStreamEndCapture(b->stream, &graph);
         if (graph) cudaGraphDestroy(graph);
@@ -239,6 +243,7 @@ int h2h_batch_rebuild(h2h_batch *b) {
     b->elim->check_error();
     b->fill->check_error();
     b->info.t_rebuild_us = event_us(b->ev[0], b->ev[3]);
+    b->info.t_rebuild_fill_us = event_us(b->ev[1], b->ev[2]);
     b->fill->attach(false);
   });
 }

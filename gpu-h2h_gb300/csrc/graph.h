@@ -198,7 +198,10 @@ struct ElimPlan {
 struct TilePolicy {
   static constexpr int kWidth = 3, kSep = 4;
   int small_work[kWidth][kSep], col_block[kWidth][kSep], sep_chunk[kWidth][kSep];
-  TilePolicy();
+  TilePolicy();  // the shallow preset
+  // the default for a forest whose deepest tree has `height` levels: the
+  // shallow preset up to 2048 levels, the deep one beyond
+  static TilePolicy for_height(int height);
   static int sep_bucket(int m) { return m <= 16 ? 0 : m <= 64 ? 1 : m <= 256 ? 2 : 3; }
   std::string str() const;
   bool parse(const std::string &s);
@@ -223,6 +226,7 @@ struct FillPlan {
   int *hld = nullptr, *htop = nullptr, *hpos = nullptr, *seg_top = nullptr, *seg_pos = nullptr;
   int64_t *seg_off = nullptr;
   int *done = nullptr, *next = nullptr, *err = nullptr, *tiles = nullptr;
+  unsigned long long *trace_t = nullptr;  // publish time per node (GPUH2H_TRACE)
   int64_t ntiles = 0, tiles_cap = 0, nchunks = 0;
   int max_u = 1, max_c = 1, max_segs = 1, blocks = 1, threads = 128;
   size_t smem = 0;
@@ -240,6 +244,7 @@ struct FillPlan {
   // rows and flags and runs the fill on s.
   void enqueue(cudaStream_t s, cudaEvent_t *fill_ev = nullptr);
   void check_error();            // synchronises; throws if a dependency wait ran out
+  void trace_report();           // GPUH2H_TRACE: the last fill's time per level class
   void attach(bool first);       // per-graph views, max_label; first: also drow_host
 };
 

@@ -226,6 +226,7 @@ struct FlowArgs {
   long long spin_limit;
   int max_u;          // max separator members in one tile (staging size)
   int max_segs;       // max root-path segments of a node (staging size)
+  unsigned long long *trace_t;  // non-null (GPUH2H_TRACE): each node's publish time, ns
 };
 
 __device__ __forceinline__ int ld_acquire(const int *p) {
@@ -340,6 +341,11 @@ __global__ void __launch_bounds__(128) fill_flow_kernel(FlowArgs A) {
       if (nt == 1 || atomicAdd(A.node_cnt + v, 1) == nt - 1) {
         __threadfence();
         st_release(A.done + v, 1);
+        if (A.trace_t) {
+          unsigned long long now;
+          asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(now));
+          A.trace_t[v] = now;
+        }
       }
     }
     __syncwarp();  // the slice is restaged only after every lane left the sweep
@@ -533,6 +539,14 @@ __global__ void build_positions_kernel(const int64_t *list_off, const int *list_
 // levels 32 x 16 above 4,096; heavy levels (the 6.26M-vertex graph's middle)
 // 128 x 256 above 16,384 -- whole separators, so no atomicMin combining.
 // Separators above 256 members always split.
+// Two measured presets.  Shallow trees (the 264k-vertex graph, tree height
+// 1,343; batches of road graphs) fill as a latency chain through the narrow
+// levels and want small tiles.  Deep trees have rows several thousand
+// columns long, so the same tiles are too many: the autotuner on the
+// 3.6M-vertex graph (height 4,180) moved the wide levels to 64-column x
+// 32-member tiles and the narrow levels' widest separators to 16-member
+// chunks, fill 1,080 -> 788 ms; on the 264k-vertex graph those shapes cost
+// 29 -> 40 ms.
 TilePolicy::TilePolicy() {
   static const int sw[kWidth] = {1024, 4096, 16384}, cb[kWidth] = {32, 32, 128}, sc[kWidth] = {4, 16, 256};
   for (int w = 0; w < kWidth; w++)
@@ -541,6 +555,21 @@ TilePolicy::TilePolicy() {
       col_block[w][b] = cb[w];
       sep_chunk[w][b] = sc[w];
     }
+}
+
+TilePolicy TilePolicy::for_height(int height) {
+  TilePolicy t;
+  if (height <= 2048) return t;
+  static const int sw[kWidth][kSep] = {{1024, 1024, 1024, 0}, {16384, 4096, 4096, 0}, {16384, 16384, 16384, 0}};
+  static const int cb[kWidth][kSep] = {{32, 32, 32, 32}, {32, 64, 64, 64}, {128, 128, 128, 128}};
+  static const int sc[kWidth][kSep] = {{4, 4, 4, 16}, {16, 32, 32, 32}, {256, 256, 256, 256}};
+  for (int w = 0; w < kWidth; w++)
+    for (int b = 0; b < kSep; b++) {
+      t.small_work[w][b] = sw[w][b];
+      t.col_block[w][b] = cb[w][b];
+      t.sep_chunk[w][b] = sc[w][b];
+    }
+  return t;
 }
 
 std::string TilePolicy::str() const {
@@ -727,8 +756,9 @@ FillPlan::FillPlan(const std::vector<Graph *> &graphs, const TilePolicy &pol, co
 FillPlan::~FillPlan() { release_work(); }
 
 void FillPlan::release_work() {
-  void *ps[] = {pos_w, pos_src, hld, htop, hpos, seg_off, seg_top, seg_pos, done, next, err, tiles};
+  void *ps[] = {pos_w, pos_src, hld, htop, hpos, seg_off, seg_top, seg_pos, done, next, err, tiles, trace_t};
   for (void *p : ps) cudaFree(p);
+  trace_t = nullptr;
   pos_w = pos_src = hld = htop = hpos = seg_top = seg_pos = done = next = err = tiles = nullptr;
   seg_off = nullptr;
 }
@@ -1010,10 +1040,65 @@ void FillPlan::enqueue(cudaStream_t s, cudaEvent_t *fill_ev) {
   A.spin_limit = spin_limit_cycles();
   A.max_u = max_u;
   A.max_segs = std::max(max_segs, 1);
-  if (fill_ev) GH_CUDA(cudaEventRecord(fill_ev[0], s));
+  A.trace_t = nullptr;
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  GH_CUDA(cudaStreamIsCapturing(s, &cs));
+  const bool capturing = cs != cudaStreamCaptureStatusNone;
+  if (std::getenv("GPUH2H_TRACE") && !capturing) {
+    if (!trace_t) GH_CUDA(cudaMalloc(&trace_t, sizeof(unsigned long long) * std::max(N, 1)));
+    GH_CUDA(cudaMemsetAsync(trace_t, 0, sizeof(unsigned long long) * std::max(N, 1), s));
+    A.trace_t = trace_t;
+  }
+  // inside a capture an event record becomes a graph node only when external
+  auto record = [&](cudaEvent_t e) {
+    GH_CUDA(capturing ? cudaEventRecordWithFlags(e, s, cudaEventRecordExternal) : cudaEventRecord(e, s));
+  };
+  if (fill_ev) record(fill_ev[0]);
   fill_flow_kernel<<<blocks, threads, smem, s>>>(A);
   GH_CUDA(cudaGetLastError());
-  if (fill_ev) GH_CUDA(cudaEventRecord(fill_ev[1], s));
+  if (fill_ev) record(fill_ev[1]);
+}
+
+// With GPUH2H_TRACE: where the last fill's time went, from the nodes'
+// publish times -- per forest level the time from the previous level's last
+// publish to its own (levels overlap in the dataflow; the spans add up to
+// the fill), summed per tile class, and the ten longest levels.
+void FillPlan::trace_report() {
+  if (!trace_t) return;
+  GH_CUDA(cudaDeviceSynchronize());
+  std::vector<unsigned long long> t(N);
+  std::vector<int> dep(N);
+  GH_CUDA(cudaMemcpy(t.data(), trace_t, sizeof(unsigned long long) * N, cudaMemcpyDeviceToHost));
+  GH_CUDA(cudaMemcpy(dep.data(), depth, sizeof(int) * N, cudaMemcpyDeviceToHost));
+  const std::vector<int> cls = level_classes();
+  const int nlev = (int)cls.size();
+  std::vector<unsigned long long> last(nlev, 0);
+  std::vector<int64_t> width(nlev, 0);
+  unsigned long long t0 = ~0ull;
+  for (int v = 0; v < N; v++) {
+    const int l = dep[v] - 1;
+    if (l < 0 || l >= nlev || t[v] == 0) continue;
+    last[l] = std::max(last[l], t[v]);
+    width[l]++;
+    t0 = std::min(t0, t[v]);
+  }
+  if (t0 == ~0ull) return;
+  double by_cls[3] = {0, 0, 0};
+  std::vector<std::pair<double, int>> spans;
+  unsigned long long prev = t0;
+  for (int l = 0; l < nlev; l++) {
+    if (!last[l]) continue;
+    const double us = last[l] > prev ? (last[l] - prev) / 1e3 : 0.0;
+    by_cls[cls[l]] += us;
+    spans.push_back({us, l});
+    prev = std::max(prev, last[l]);
+  }
+  std::fprintf(stderr, "[gpuh2h] fill trace: first to last publish %.3f ms; narrow levels %.3f, wide %.3f, heavy %.3f ms\n",
+               (prev - t0) / 1e6, by_cls[0] / 1e3, by_cls[1] / 1e3, by_cls[2] / 1e3);
+  std::sort(spans.rbegin(), spans.rend());
+  for (size_t k = 0; k < spans.size() && k < 10; k++)
+    std::fprintf(stderr, "[gpuh2h] fill trace: level %d (class %d, %lld nodes): %.1f us\n", spans[k].second,
+                 cls[spans[k].second], (long long)width[spans[k].second], spans[k].first);
 }
 
 void FillPlan::check_error() {
@@ -1147,7 +1232,7 @@ void fill_labels_gpu(Graph &g) {
   // keeps the level-synchronous kernel that applies the reference's order.
   const bool flow = !uses_level_fill(g);
   if (flow) {
-    TilePolicy pol;
+    TilePolicy pol = TilePolicy::for_height(g.tree_height);
     if (const char *e = std::getenv("GPUH2H_TILE_POLICY"))
       GH_CHECK(pol.parse(e), H2H_ERR_ARG, "GPUH2H_TILE_POLICY: expected 12 entries small_work/col_block/sep_chunk");
     FillPlan plan({&g}, pol, D.lists);
@@ -1161,6 +1246,7 @@ void fill_labels_gpu(Graph &g) {
     try {
       plan.enqueue(0, ev);
       plan.check_error();
+      plan.trace_report();
       GH_CUDA(cudaEventElapsedTime(&ms, ev[0], ev[1]));
     } catch (...) {
       cudaEventDestroy(ev[0]);
