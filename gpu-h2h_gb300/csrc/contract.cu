@@ -236,7 +236,15 @@ __device__ void merge_neighbour(const ElimArgs &A, int u, const NbrMeta &m, int 
       }
     }
   }
-  if (fits) {
+  if (fits && total == np && Jn == 0) {
+    // no insert (every member of Q is already in P, as near the top of the
+    // order): the output is P with its matched entries min-updated by pass
+    // 1, written contiguously
+    for (int k = lane; k < np; k += 32) {
+      A.slot_nbr[off + k] = pid[k];
+      A.slot_w[off + k] = pw[k];
+    }
+  } else if (fits) {
     int o = incl - cnt;
     int i = i0, j = k0 - i0;
     for (int t = k0; t < k1; t++) {
@@ -274,7 +282,9 @@ __device__ void merge_neighbour(const ElimArgs &A, int u, const NbrMeta &m, int 
   __syncwarp();
 }
 
-__global__ void __launch_bounds__(512) elim_kernel(ElimArgs A) {
+// 48 registers: five 8-warp CTAs per SM for the many small cells at the
+// bottom (left to itself the compiler takes 56 and fits four)
+__global__ void __maxnreg__(48) elim_kernel(ElimArgs A) {
   extern __shared__ __align__(16) unsigned char smem[];
   cg::cluster_group cluster = cg::this_cluster();
   const int CS = (int)cluster.num_blocks();
