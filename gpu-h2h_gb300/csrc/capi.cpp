@@ -215,6 +215,8 @@ int h2h_query_batch_host(const h2h_graph *hc, const int *x, const int *y, int *o
     gh::HostQueryStage &s = h->stage;
     std::lock_guard<std::mutex> lock(s.mu);
     if (!s.stream) GH_CUDA(cudaStreamCreateWithFlags(&s.stream, cudaStreamNonBlocking));
+    if (!s.stream2) GH_CUDA(cudaStreamCreateWithFlags(&s.stream2, cudaStreamNonBlocking));
+    if (!s.joined) GH_CUDA(cudaEventCreateWithFlags(&s.joined, cudaEventDisableTiming));
     if (n > s.cap) {
       cudaFree(s.dx); cudaFree(s.dy); cudaFree(s.dout);
       s.dx = s.dy = s.dout = nullptr;
@@ -224,10 +226,24 @@ int h2h_query_batch_host(const h2h_graph *hc, const int *x, const int *y, int *o
       GH_CUDA(cudaMalloc(&s.dout, sizeof(int) * n));
       s.cap = n;
     }
-    GH_CUDA(cudaMemcpyAsync(s.dx, x, sizeof(int) * n, cudaMemcpyHostToDevice, s.stream));
-    GH_CUDA(cudaMemcpyAsync(s.dy, y, sizeof(int) * n, cudaMemcpyHostToDevice, s.stream));
-    gh::run_query_batch(g, s.dx, s.dy, s.dout, n, mode, s.stream);
-    GH_CUDA(cudaMemcpyAsync(out, s.dout, sizeof(int) * n, cudaMemcpyDeviceToHost, s.stream));
+    // A batch of a million pairs or more goes in up to four chunks on two
+    // alternating streams, so one chunk's copies overlap another's queries;
+    // a chunk keeps at least half a million pairs (a full wave of 32-query
+    // warp tiles).  Smaller batches are one chunk (the latency path).
+    const int64_t chunk = n >= (int64_t(1) << 20) ? std::max<int64_t>(int64_t(1) << 19, (n + 3) / 4) : n;
+    int k = 0;
+    for (int64_t a = 0; a < n; a += chunk, k++) {
+      const int64_t c = std::min(chunk, n - a);
+      cudaStream_t st = (k & 1) ? s.stream2 : s.stream;
+      GH_CUDA(cudaMemcpyAsync(s.dx + a, x + a, sizeof(int) * c, cudaMemcpyHostToDevice, st));
+      GH_CUDA(cudaMemcpyAsync(s.dy + a, y + a, sizeof(int) * c, cudaMemcpyHostToDevice, st));
+      gh::run_query_batch(g, s.dx + a, s.dy + a, s.dout + a, c, mode, st);
+      GH_CUDA(cudaMemcpyAsync(out + a, s.dout + a, sizeof(int) * c, cudaMemcpyDeviceToHost, st));
+    }
+    if (k > 1) {  // the flag read waits for both streams
+      GH_CUDA(cudaEventRecord(s.joined, s.stream2));
+      GH_CUDA(cudaStreamWaitEvent(s.stream, s.joined, 0));
+    }
     int bad = 0;
     GH_CUDA(cudaMemcpyAsync(&bad, g.dev.err, sizeof(int), cudaMemcpyDeviceToHost, s.stream));
     GH_CUDA(cudaStreamSynchronize(s.stream));

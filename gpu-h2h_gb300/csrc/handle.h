@@ -17,10 +17,13 @@ struct HostQueryStage {
   std::mutex mu;
   int *dx = nullptr, *dy = nullptr, *dout = nullptr;
   int64_t cap = 0;
-  cudaStream_t stream = nullptr;
+  cudaStream_t stream = nullptr, stream2 = nullptr;  // large batches alternate chunks between them
+  cudaEvent_t joined = nullptr;
   ~HostQueryStage() {
     cudaFree(dx); cudaFree(dy); cudaFree(dout);
     if (stream) cudaStreamDestroy(stream);
+    if (stream2) cudaStreamDestroy(stream2);
+    if (joined) cudaEventDestroy(joined);
   }
 };
 
