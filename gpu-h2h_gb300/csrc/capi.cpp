@@ -226,11 +226,11 @@ int h2h_query_batch_host(const h2h_graph *hc, const int *x, const int *y, int *o
       GH_CUDA(cudaMalloc(&s.dout, sizeof(int) * n));
       s.cap = n;
     }
-    // A batch of a million pairs or more goes in up to four chunks on two
+    // A batch of a million pairs or more goes in up to eight chunks on two
     // alternating streams, so one chunk's copies overlap another's queries;
-    // a chunk keeps at least half a million pairs (a full wave of 32-query
-    // warp tiles).  Smaller batches are one chunk (the latency path).
-    const int64_t chunk = n >= (int64_t(1) << 20) ? std::max<int64_t>(int64_t(1) << 19, (n + 3) / 4) : n;
+    // a chunk keeps at least a quarter million pairs.  Smaller batches are
+    // one chunk (the latency path).
+    const int64_t chunk = n >= (int64_t(1) << 20) ? std::max<int64_t>(int64_t(1) << 18, (n + 7) / 8) : n;
     int k = 0;
     for (int64_t a = 0; a < n; a += chunk, k++) {
       const int64_t c = std::min(chunk, n - a);
