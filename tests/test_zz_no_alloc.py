@@ -66,3 +66,43 @@ def test_noalloc_fill_matches_regular_path_twice(cfg0_root):
                                       dev["dis_hash"].data_ptr(), 1 << 23, out.data_ptr(), max_depth, max_sep,
                                       s.cuda_stream)
     assert e.value.code == -1
+
+
+def test_noalloc_fill_wait_runs_out_then_recovers(cfg0_root):
+    """A dependency that never completes ends the fill with an error status
+    instead of a hang: the order below drops the root (its children wait for
+    a flag that nothing sets) and every wait is bounded (about 2 s), so the
+    kernel returns H2H_ERR_DEVICE; the context stays usable and the next call,
+    with the proper order, writes the regular path's labels."""
+    import torch
+
+    import gpuh2h
+    g = gpuh2h.Graph("t", 6, 1, 4, 1, files=gpuh2h.files_for(cfg0_root, "cfg0"))
+    g.contraction_noHub(1)
+    g.constructLabel_noHub(2, 1, gpuh2h.LABEL_L4)
+    host, expected = _inputs(g)
+    broken = host["order"].copy()
+    assert host["father"][broken[0]] < 0  # the level order starts at the root
+    broken[0] = broken[1]                 # the root is never filled
+    dev = {k: torch.from_numpy(np.ascontiguousarray(v)).cuda() for k, v in host.items()}
+    d_broken = torch.from_numpy(np.ascontiguousarray(broken)).cuda()
+    n = len(host["father"])
+    total = int(host["dis_hash"][-1])
+    max_depth = int(host["depth"].max())
+    max_sep = int((np.diff(host["pos_hash"]) - 1).max())
+    out = torch.full((total,), -7, dtype=torch.int32, device="cuda")
+    s = torch.cuda.current_stream()
+
+    def run(order):
+        gpuh2h.fill_labels_l4_noalloc(n, order.data_ptr(), dev["father"].data_ptr(), dev["depth"].data_ptr(),
+                                      dev["pos_hash"].data_ptr(), dev["pos_id"].data_ptr(),
+                                      dev["pos_pos"].data_ptr(), dev["pos_w"].data_ptr(),
+                                      dev["dis_hash"].data_ptr(), total, out.data_ptr(), max_depth, max_sep,
+                                      s.cuda_stream)
+
+    with pytest.raises(gpuh2h.H2HError) as e:
+        run(d_broken)
+    assert e.value.code == -8 and "wait ran out" in str(e.value)
+    out.fill_(-7)
+    run(dev["order"])
+    assert np.array_equal(out.cpu().numpy(), expected)
