@@ -118,12 +118,10 @@ __device__ __forceinline__ int corank(const int *pid, int np, const int *aid, in
   return lo;
 }
 
-// What a merge needs to know about neighbour u: list start, length (junk
-// prefix included), junk prefix, and -- loaded up front in the same round
-// trip when kPre, else where they are used -- capacity, height, candidate
-// index.  Only the warp merging u writes these during an elimination (the
-// candidate index changes only when u is picked).  kPre costs registers: the
-// cluster kernel, which wants several CTAs per SM, loads late.
+// What a merge needs to know about neighbour u, loaded in one round trip:
+// list start, length (junk prefix included), junk prefix, capacity, height,
+// candidate index.  Only the warp merging u writes these during an
+// elimination (the candidate index changes only when u is picked).
 struct NbrMeta {
   int64_t off;
   int s, J, cap, h, p;
@@ -131,17 +129,14 @@ struct NbrMeta {
 
 // Mutable global data is read through L2 (ld.global.cg): other CTAs write it
 // between barriers.
-template <bool kPre>
 __device__ __forceinline__ NbrMeta load_meta(const ElimArgs &A, int u) {
   NbrMeta m;
   m.off = __ldcg(A.slot_off + u);
   m.s = __ldcg(A.lsize + u);
   m.J = __ldcg(A.ljunk + u);
-  if (kPre) {
-    m.cap = __ldcg(A.cap + u);
-    m.h = __ldcg(A.height + u);
-    m.p = __ldcg(A.cpos + u);
-  }
+  m.cap = __ldcg(A.cap + u);
+  m.h = __ldcg(A.height + u);
+  m.p = __ldcg(A.cpos + u);
   return m;
 }
 
@@ -149,7 +144,6 @@ __device__ __forceinline__ NbrMeta load_meta(const ElimArgs &A, int u) {
 //   P = valid entries of u's list except v (kernel_functions.cu:364-390),
 //   output = P with the first entry of every matched id min-updated, plus the
 //   unmatched members of Q inserted in order (:392-457).
-template <bool kPre>
 __device__ void merge_neighbour(const ElimArgs &A, int u, const NbrMeta &m, int wu, int iu, int v, int hnow,
                                 const int *aid, const int *aw, int c, int *pid, int *pw, int lane, Cand cand,
                                 int nslots) {
@@ -215,7 +209,7 @@ __device__ void merge_neighbour(const ElimArgs &A, int u, const NbrMeta &m, int 
     if (lane >= o) incl += y;
   }
   const int total = __shfl_sync(0xffffffffu, incl, 31);
-  const int capu = kPre ? m.cap : __ldcg(A.cap + u);
+  const int capu = m.cap;
   bool fits = Jn + total <= capu;
   if (!fits && A.heap_mode) {
     // the reference's heap adjacency is a hash map that grows freely: move the
@@ -270,10 +264,10 @@ __device__ void merge_neighbour(const ElimArgs &A, int u, const NbrMeta &m, int 
     const int ns = fits ? Jn + total : s;
     A.lsize[u] = ns;
     A.ljunk[u] = fits ? Jn : J;
-    const int h = kPre ? m.h : __ldcg(A.height + u);
+    const int h = m.h;
     const int hn = (hnow + 1 > h) ? hnow + 1 : h;
     A.height[u] = hn;
-    const int p = kPre ? m.p : __ldcg(A.cpos + u);
+    const int p = m.p;
     if (p >= 0 && p < nslots) {  // a remaining candidate of this cell: refresh its key
       cand.deg[p] = ns;
       cand.third[p] = hn;
@@ -433,12 +427,12 @@ __global__ void __maxnreg__(48) elim_kernel(ElimArgs A) {
       }
       for (int i = rank * nw + wid; i < c; i += CS * nw) {
         const int u = aid[i];
-        const NbrMeta m = load_meta<false>(A, u);
+        const NbrMeta m = load_meta(A, u);
         if (m.s - m.J > A.lmax) {
           if (lane == 0) set_err(A.err, kErrStaging);
           continue;
         }
-        merge_neighbour<false>(A, u, m, aw[i], i, v, hnow, aid, aw, c, pid, pw, lane, lead, k);
+        merge_neighbour(A, u, m, aw[i], i, v, hnow, aid, aw, c, pid, pw, lane, lead, k);
       }
     }
     cluster.sync();  // no CTA leaves while a peer may still read the leader's shared memory
@@ -711,12 +705,12 @@ __global__ void __launch_bounds__(512, 1) cell_grid_kernel(GridArgs H) {
     for (int t = wid; t < nm; t += nw) {
       const int i = mine[t];
       const int u = aid[i];
-      const NbrMeta m = load_meta<true>(A, u);
+      const NbrMeta m = load_meta(A, u);
       if (m.s - m.J > A.lmax) {
         if (lane == 0) set_err(A.err, kErrStaging);
         continue;
       }
-      merge_neighbour<true>(A, u, m, aw[i], i, v, hnow, aid, aw, c, pid, pw, lane, cand, ns);
+      merge_neighbour(A, u, m, aw[i], i, v, hnow, aid, aw, c, pid, pw, lane, cand, ns);
     }
     __syncthreads();
     // ---- after the first pick of a partition cell every key becomes live
