@@ -370,6 +370,16 @@ int h2h_copy_input_arcs(const h2h_graph *h, int *adj_off, int *adj_v, int *adj_w
   });
 }
 
+int h2h_copy_partition(const h2h_graph *h, int *part_ids, int *id_hash) {
+  if (!h) { gh::set_last_error("null handle"); return H2H_ERR_ARG; }
+  return guarded([&] {
+    const gh::Graph &g = h->g;
+    GH_CHECK((int)g.part_ids.size() == g.n, H2H_ERR_STATE, "no partition array (a loaded index has none)");
+    if (part_ids) std::copy(g.part_ids.begin(), g.part_ids.end(), part_ids);
+    if (id_hash) std::copy(g.id_hash.begin(), g.id_hash.end(), id_hash);
+  });
+}
+
 int h2h_copy_bfs(const h2h_graph *h, int *tree_bfs, int *tree_hash) {
   if (!h) { gh::set_last_error("null handle"); return H2H_ERR_ARG; }
   return guarded([&] {

@@ -129,17 +129,109 @@ bool parse_arcs_parallel(const Cursor &c0, long long m, int n, int threads, std:
     if (total >= m) break;
   }
   if (total < m) return false;
-  eu.reserve(m);
-  ev.reserve(m);
-  ew.reserve(m);
-  long long taken = 0;
-  for (int t = 0; t < T && taken < m; t++)
-    for (size_t i = 0; i < parts[t].u.size() && taken < m; i++, taken++) {
-      if (parts[t].u[i] == parts[t].v[i]) continue;  // self loops dropped
-      eu.push_back(parts[t].u[i]);
-      ev.push_back(parts[t].v[i]);
-      ew.push_back(parts[t].w[i]);
+  // the first m arcs, self loops dropped, in file order: per part the arcs
+  // it contributes and where they land, then the copies in parallel
+  std::vector<long long> take(T, 0), keep(T, 0), at(T + 1, 0);
+  long long left = m;
+  for (int t = 0; t < T; t++) {
+    take[t] = std::min<long long>(left, (long long)parts[t].u.size());
+    left -= take[t];
+  }
+  pool.parallel_for(T, 1, [&](int64_t lo, int64_t hi, int) {
+    for (int64_t t = lo; t < hi; t++) {
+      long long k = 0;
+      for (long long i = 0; i < take[t]; i++) k += parts[t].u[i] != parts[t].v[i];
+      keep[t] = k;
     }
+  });
+  for (int t = 0; t < T; t++) at[t + 1] = at[t] + keep[t];
+  eu.resize(at[T]);
+  ev.resize(at[T]);
+  ew.resize(at[T]);
+  pool.parallel_for(T, 1, [&](int64_t lo, int64_t hi, int) {
+    for (int64_t t = lo; t < hi; t++) {
+      long long o = at[t];
+      for (long long i = 0; i < take[t]; i++) {
+        if (parts[t].u[i] == parts[t].v[i]) continue;  // self loops dropped
+        eu[o] = parts[t].u[i];
+        ev[o] = parts[t].v[i];
+        ew[o] = parts[t].w[i];
+        o++;
+      }
+    }
+  });
+  return true;
+}
+
+// The (position, vertex) pairs of an ID file in parallel, for files with one
+// vertex per line ("idx lon lat vid"): chunks cut at line starts, each parsed
+// on its own.  Returns false (nothing set) when the file needs the
+// token-by-token reader -- a record spread over lines, fewer than n records,
+// anything unparsable; positions or ids out of range raise H2H_ERR_FORMAT.
+bool parse_ids_parallel(const Cursor &c0, int n, int threads, std::vector<int> &part_ids,
+                        std::vector<int> &id_hash) {
+  const char *b = c0.p, *e = c0.e;
+  if (threads < 2 || e - b < (1 << 20)) return false;
+  const int T = threads;
+  std::vector<const char *> cut(T + 1, e);
+  cut[0] = b;
+  for (int t = 1; t < T; t++) {
+    const char *q = b + (e - b) * t / T;
+    while (q < e && *q != '\n') q++;
+    cut[t] = q < e ? q + 1 : e;
+  }
+  struct Part {
+    std::vector<int> hash, id;
+    bool ok = true, range = true;
+  };
+  std::vector<Part> parts(T);
+  Pool pool(T);
+  pool.parallel_for(T, 1, [&](int64_t lo, int64_t hi, int) {
+    for (int64_t t = lo; t < hi; t++) {
+      Part &P = parts[t];
+      static const std::string kEmpty;
+      Cursor c(kEmpty, c0.what);
+      c.p = cut[t];
+      c.e = cut[t + 1];
+      try {
+        for (;;) {
+          c.skip();
+          if (c.p >= c.e) break;
+          const long long hash = c.integer();
+          c.token();
+          c.token();
+          const long long id = c.integer();
+          if (hash < 0 || hash >= n || id < 0 || id >= n) { P.range = false; break; }
+          P.hash.push_back((int)hash);
+          P.id.push_back((int)id);
+          const char *q = c.p;  // a record must end its line
+          while (q < c.e && (*q == ' ' || *q == '\t' || *q == '\r')) q++;
+          if (q < c.e && *q != '\n') { P.ok = false; break; }
+        }
+      } catch (const Error &) {
+        P.ok = false;
+      }
+    }
+  });
+  long long total = 0;
+  std::vector<long long> take(T, 0);
+  for (int t = 0; t < T && total < n; t++) {
+    if (!parts[t].ok) return false;
+    take[t] = std::min<long long>(n - total, (long long)parts[t].hash.size());
+    if (!parts[t].range && total + take[t] < n)
+      throw Error(H2H_ERR_FORMAT, "index out of range in " + c0.what);
+    total += take[t];
+  }
+  if (total < n) return false;
+  // records of one position or id twice leave another unset: the caller's
+  // permutation check rejects the file
+  pool.parallel_for(T, 1, [&](int64_t lo, int64_t hi, int) {
+    for (int64_t t = lo; t < hi; t++)
+      for (long long i = 0; i < take[t]; i++) {
+        part_ids[parts[t].hash[i]] = parts[t].id[i];
+        id_hash[parts[t].id[i]] = parts[t].hash[i];
+      }
+  });
   return true;
 }
 
@@ -158,14 +250,18 @@ void load_graph(Graph &g, const std::string &edge, const std::string &idf, const
     g.n = (int)n;
     g.part_ids.assign(g.n, -1);
     g.id_hash.assign(g.n, -1);
-    for (int i = 0; i < g.n; i++) {                       // :27-31
-      long long hash = c.integer();
-      c.token();
-      c.token();
-      long long id = c.integer();
-      GH_CHECK(hash >= 0 && hash < n && id >= 0 && id < n, H2H_ERR_FORMAT, "index out of range in " + idf);
-      g.part_ids[hash] = (int)id;
-      g.id_hash[id] = (int)hash;
+    if (!parse_ids_parallel(c, g.n, std::max(1, g.threads), g.part_ids, g.id_hash)) {
+      std::fill(g.part_ids.begin(), g.part_ids.end(), -1);
+      std::fill(g.id_hash.begin(), g.id_hash.end(), -1);
+      for (int i = 0; i < g.n; i++) {                     // :27-31
+        long long hash = c.integer();
+        c.token();
+        c.token();
+        long long id = c.integer();
+        GH_CHECK(hash >= 0 && hash < n && id >= 0 && id < n, H2H_ERR_FORMAT, "index out of range in " + idf);
+        g.part_ids[hash] = (int)id;
+        g.id_hash[id] = (int)hash;
+      }
     }
     for (int i = 0; i < g.n; i++)
       GH_CHECK(g.part_ids[i] >= 0 && g.id_hash[i] >= 0, H2H_ERR_FORMAT, idf + " is not a permutation");

@@ -108,6 +108,7 @@ SIGNATURES = {
     "h2h_fill_labels_l4_noalloc": (_i32, [_i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i64, _vp, _i32, _i32,
                                           _vp]),
     "h2h_copy_input_arcs": (_i32, [_vp, _vp, _vp, _vp]),
+    "h2h_copy_partition": (_i32, [_vp, _vp, _vp]),
     "h2h_save_index": (_i32, [_vp, _cp]),
     "h2h_fill_labels_plain": (_i32, [_vp, C.POINTER(C.c_double), C.POINTER(_i64)]),
     "h2h_fill_labels_plain_node": (_i32, [_vp, C.POINTER(C.c_double), C.POINTER(_i64)]),
@@ -364,6 +365,15 @@ class Graph:
         w = np.empty(i["m"], np.int32)
         _check(self._L.h2h_copy_input_arcs(self.h, _p(off), _p(v), _p(w)))
         return off, v, w
+
+    def partition(self):
+        """(part_ids, id_hash): the vertex at each partition position and the
+        position of each vertex, as the ID file gives them."""
+        n = self.info()["n"]
+        part = np.empty(n, np.int32)
+        pos = np.empty(n, np.int32)
+        _check(self._L.h2h_copy_partition(self.h, _p(part), _p(pos)))
+        return part, pos
 
     def local_pairs(self, n: int, max_hops: int = 20, seed: int = 1):
         x = np.empty(n, np.int32)

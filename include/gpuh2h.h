@@ -269,6 +269,11 @@ int h2h_load_index(const char *path, h2h_graph **out);
  * adj_off[n+1], adj_v[m], adj_w[m]. */
 int h2h_copy_input_arcs(const h2h_graph *g, int *adj_off, int *adj_v, int *adj_w);
 
+/* The partition array of a loaded graph as the ID file gives it
+ * (Graph_Fundamental.cu:27-31): part_ids[idx] = NE_P[idx].NodeID (the vertex
+ * at partition position idx) and id_hash[vertex] = idx, n entries each. */
+int h2h_copy_partition(const h2h_graph *g, int *part_ids, int *id_hash);
+
 #ifdef __cplusplus
 }
 #endif

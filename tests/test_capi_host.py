@@ -176,3 +176,46 @@ def test_index_file_validation(tmp_path):
     incons.write_bytes(b"GPUH2HIX" + struct.pack("<II", 1, 16) + hdr + struct.pack("<I", 0))
     assert L.h2h_load_index(str(incons).encode(), C.byref(h)) == -3
     assert not h
+
+
+def test_parallel_loader_equals_serial(tmp_path):
+    """Files big enough for the chunked parsers (over 1 MB: 60k vertices)
+    load to exactly what the one-token-at-a-time reader gives: partition
+    array, CSR arcs in file order.  A file whose records break the one-per-line
+    layout falls back to the token reader and still loads the same; a
+    duplicated ID record is rejected either way."""
+    import gpuh2h
+    root = str(tmp_path)
+    gpuh2h.generate_road(root, "p", n=60000, target_arcs=170000, aspect_milli=1300, jitter_milli=300,
+                         diag_permille=50, hw_tiers=1, hw_permille10=50, hw_k=3, hw_scale_milli=400,
+                         partition_height=8, seed=5, cols=0, drop_permille=0)
+    files = gpuh2h.files_for(root, "p")
+    assert os.path.getsize(files[0]) > (1 << 20) and os.path.getsize(files[1]) > (1 << 20)
+
+    def load(fs, threads):
+        g = gpuh2h.Graph("p", 8, 2, threads, 1, files=fs)
+        out = g.partition() + g.input_arcs()
+        g.close()
+        return out
+
+    serial = load(files, 1)
+    for a, b in zip(serial, load(files, 8)):
+        assert np.array_equal(a, b)
+    # one ID record split over two lines: the chunked reader declines, the token reader agrees
+    idf = open(files[1]).read().split("\n")
+    idf[5] = idf[5].replace(" ", "\n", 1)
+    split = str(tmp_path / "split_ID.txt")
+    with open(split, "w") as f:
+        f.write("\n".join(idf))
+    for a, b in zip(serial, load((files[0], split, files[2]), 8)):
+        assert np.array_equal(a, b)
+    # a position given twice leaves another unset: not a permutation
+    idf = open(files[1]).read().split("\n")
+    first, second = idf[1].split(), idf[2].split()
+    idf[2] = " ".join([first[0]] + second[1:])
+    dup = str(tmp_path / "dup_ID.txt")
+    with open(dup, "w") as f:
+        f.write("\n".join(idf))
+    for threads in (1, 8):
+        rc, h = _load((files[0], dup, files[2]), H=8, Cg=2, threads=threads)
+        assert rc == -3 and not h
