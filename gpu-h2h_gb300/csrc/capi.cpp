@@ -232,13 +232,19 @@ int h2h_query_batch_host(const h2h_graph *hc, const int *x, const int *y, int *o
     // one chunk (the latency path).
     const int64_t chunk = n >= (int64_t(1) << 20) ? std::max<int64_t>(int64_t(1) << 18, (n + 7) / 8) : n;
     int k = 0;
-    for (int64_t a = 0; a < n; a += chunk, k++) {
-      const int64_t c = std::min(chunk, n - a);
-      cudaStream_t st = (k & 1) ? s.stream2 : s.stream;
-      GH_CUDA(cudaMemcpyAsync(s.dx + a, x + a, sizeof(int) * c, cudaMemcpyHostToDevice, st));
-      GH_CUDA(cudaMemcpyAsync(s.dy + a, y + a, sizeof(int) * c, cudaMemcpyHostToDevice, st));
-      gh::run_query_batch(g, s.dx + a, s.dy + a, s.dout + a, c, mode, st);
-      GH_CUDA(cudaMemcpyAsync(out + a, s.dout + a, sizeof(int) * c, cudaMemcpyDeviceToHost, st));
+    try {
+      for (int64_t a = 0; a < n; a += chunk, k++) {
+        const int64_t c = std::min(chunk, n - a);
+        cudaStream_t st = (k & 1) ? s.stream2 : s.stream;
+        GH_CUDA(cudaMemcpyAsync(s.dx + a, x + a, sizeof(int) * c, cudaMemcpyHostToDevice, st));
+        GH_CUDA(cudaMemcpyAsync(s.dy + a, y + a, sizeof(int) * c, cudaMemcpyHostToDevice, st));
+        gh::run_query_batch(g, s.dx + a, s.dy + a, s.dout + a, c, mode, st);
+        GH_CUDA(cudaMemcpyAsync(out + a, s.dout + a, sizeof(int) * c, cudaMemcpyDeviceToHost, st));
+      }
+    } catch (...) {  // nothing of this call may still run when the next one reuses the buffers
+      cudaStreamSynchronize(s.stream);
+      cudaStreamSynchronize(s.stream2);
+      throw;
     }
     if (k > 1) {  // the flag read waits for both streams
       GH_CUDA(cudaEventRecord(s.joined, s.stream2));
