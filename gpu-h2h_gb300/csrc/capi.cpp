@@ -6,6 +6,7 @@
 #include <mutex>
 #include <string>
 
+#include "gen.h"
 #include "gpuh2h_tools.h"
 #include "handle.h"
 
@@ -15,9 +16,6 @@ void write_contract_csv(const Graph &g, const std::string &root);
 void write_construct_info(const Graph &g, const std::string &root);
 void write_query_result(const Graph &g, const std::string &root, int64_t qn, const int64_t *t19);
 const char *partition_file_prefix(int method);
-void generate_road(const h2h_gen_params &p, const std::string &root, const std::string &name, int64_t *n_arcs);
-void gen_uniform_pairs(int nv, int64_t n, uint64_t seed, int *x, int *y);
-void gen_local_pairs(const Graph &g, int64_t n, int hops, uint64_t seed, int *x, int *y);
 
 static thread_local std::string g_last_error;
 void set_last_error(const std::string &msg) { g_last_error = msg; }
@@ -217,6 +215,10 @@ int h2h_query_batch_host(const h2h_graph *hc, const int *x, const int *y, int *o
     if (!s.stream) GH_CUDA(cudaStreamCreateWithFlags(&s.stream, cudaStreamNonBlocking));
     if (!s.stream2) GH_CUDA(cudaStreamCreateWithFlags(&s.stream2, cudaStreamNonBlocking));
     if (!s.joined) GH_CUDA(cudaEventCreateWithFlags(&s.joined, cudaEventDisableTiming));
+    if (!s.dbad) {
+      GH_CUDA(cudaMalloc(&s.dbad, sizeof(int)));
+      GH_CUDA(cudaMemsetAsync(s.dbad, 0, sizeof(int), s.stream));
+    }
     if (n > s.cap) {
       cudaFree(s.dx); cudaFree(s.dy); cudaFree(s.dout);
       s.dx = s.dy = s.dout = nullptr;
@@ -238,7 +240,7 @@ int h2h_query_batch_host(const h2h_graph *hc, const int *x, const int *y, int *o
         cudaStream_t st = (k & 1) ? s.stream2 : s.stream;
         GH_CUDA(cudaMemcpyAsync(s.dx + a, x + a, sizeof(int) * c, cudaMemcpyHostToDevice, st));
         GH_CUDA(cudaMemcpyAsync(s.dy + a, y + a, sizeof(int) * c, cudaMemcpyHostToDevice, st));
-        gh::run_query_batch(g, s.dx + a, s.dy + a, s.dout + a, c, mode, st);
+        gh::run_query_batch(g, s.dx + a, s.dy + a, s.dout + a, c, mode, st, s.dbad);
         GH_CUDA(cudaMemcpyAsync(out + a, s.dout + a, sizeof(int) * c, cudaMemcpyDeviceToHost, st));
       }
     } catch (...) {  // nothing of this call may still run when the next one reuses the buffers
@@ -251,10 +253,10 @@ int h2h_query_batch_host(const h2h_graph *hc, const int *x, const int *y, int *o
       GH_CUDA(cudaStreamWaitEvent(s.stream, s.joined, 0));
     }
     int bad = 0;
-    GH_CUDA(cudaMemcpyAsync(&bad, g.dev.err, sizeof(int), cudaMemcpyDeviceToHost, s.stream));
+    GH_CUDA(cudaMemcpyAsync(&bad, s.dbad, sizeof(int), cudaMemcpyDeviceToHost, s.stream));
     GH_CUDA(cudaStreamSynchronize(s.stream));
     if (bad) {
-      GH_CUDA(cudaMemsetAsync(g.dev.err, 0, sizeof(int), s.stream));
+      GH_CUDA(cudaMemsetAsync(s.dbad, 0, sizeof(int), s.stream));
       GH_CUDA(cudaStreamSynchronize(s.stream));
       throw gh::Error(H2H_ERR_ARG, "vertex id out of range in batch (those pairs answered -1)");
     }
@@ -416,18 +418,7 @@ int h2h_write_query_result(const h2h_graph *h, const char *root, int64_t query_n
 // ------------------------------------------------------------ tools
 
 void h2h_gen_default(h2h_gen_params *p) {
-  if (!p) return;
-  std::memset(p, 0, sizeof(*p));
-  p->n = 4096;
-  p->cols = 64;
-  p->aspect_milli = 1000;
-  p->jitter_milli = 300;
-  p->drop_permille = 100;
-  p->diag_permille = 50;
-  p->hw_k = 3;
-  p->hw_scale_milli = 400;
-  p->partition_height = 6;
-  p->seed = 20240601;
+  if (p) gh::gen_default(p);
 }
 
 int h2h_generate_road(const h2h_gen_params *p, const char *root, const char *name, int64_t *n_arcs) {
@@ -447,7 +438,7 @@ int h2h_gen_local_pairs(const h2h_graph *h, int64_t n, int max_hops, uint64_t se
     gh::set_last_error("the input arcs are not loaded (an index read by h2h_load_index has none)");
     return H2H_ERR_STATE;
   }
-  gh::gen_local_pairs(h->g, n, max_hops, seed, x, y);
+  gh::gen_local_pairs_csr(h->g.n, h->g.adj_off.data(), h->g.adj_v.data(), n, max_hops, seed, x, y);
   return H2H_OK;
 }
 

@@ -13,15 +13,9 @@
 #include <string>
 
 #include "gpuh2h.h"
+#include "status.h"
 
 namespace gh {
-
-// Raised inside the library; capi.cpp converts it into a status code and the
-// last-error string.  Nothing crosses the C ABI as an exception.
-struct Error : std::runtime_error {
-  int code;
-  Error(int c, const std::string &m) : std::runtime_error(m), code(c) {}
-};
 
 void set_last_error(const std::string &msg);
 
@@ -31,11 +25,6 @@ void set_last_error(const std::string &msg);
     if (e_ != cudaSuccess)                                                                         \
       throw ::gh::Error(H2H_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_) + " (" + \
                                           __FILE__ + ":" + std::to_string(__LINE__) + ")");        \
-  } while (0)
-
-#define GH_CHECK(cond, code, msg)                 \
-  do {                                            \
-    if (!(cond)) throw ::gh::Error((code), (msg)); \
   } while (0)
 
 struct Clock {

@@ -19,8 +19,9 @@ struct HostQueryStage {
   int64_t cap = 0;
   cudaStream_t stream = nullptr, stream2 = nullptr;  // large batches alternate chunks between them
   cudaEvent_t joined = nullptr;
+  int *dbad = nullptr;  // this path's own out-of-range flag (device batches on the graph never touch it)
   ~HostQueryStage() {
-    cudaFree(dx); cudaFree(dy); cudaFree(dout);
+    cudaFree(dx); cudaFree(dy); cudaFree(dout); cudaFree(dbad);
     if (stream) cudaStreamDestroy(stream);
     if (stream2) cudaStreamDestroy(stream2);
     if (joined) cudaEventDestroy(joined);

@@ -2,16 +2,19 @@
 // memory: h2h_fill_labels_l4_noalloc (include/gpuh2h.h).
 //
 // Some callers cannot call cudaMalloc: code that runs inside another
-// framework's memory budget or its graph-capture region, embedded services
-// whose device memory is partitioned up front, or plugins that may only use
-// the buffers their host hands them.  This entry point takes every input and
+// framework's memory budget, embedded services whose device memory is
+// partitioned up front, or plugins that may only use the buffers their host
+// hands them.  This entry point takes every input and
 // the output as caller-owned device buffers and keeps the fill's scratch (one
 // "finished" flag per tree node, a work counter, an error word and the
 // ancestor chain of every node) in one file-scope __device__ array of
 // kScratchInts ints (32 MiB).  Every GPU that loads the library holds that
 // array until the process exits.
 //
-// The fill itself is the dataflow form of the L4 label fill (labels.cu):
+// A first kernel checks every caller-passed offset, id and depth against the
+// declared sizes and sets the error word before anything else is written;
+// the fill kernel does no work once that word is set.  The fill itself is
+// the dataflow form of the L4 label fill (labels.cu):
 // persistent CTAs take nodes in the caller's order, wait for the father's
 // flag (bounded spin with an error exit), stage the node's separator and
 // ancestor rows in shared memory and compute each label column as the exact
@@ -43,7 +46,7 @@ struct NoAllocArgs {
   int64_t total_label;
   int *done;   // scratch: n flags
   int *next;   // scratch: work counter
-  int *err;    // scratch: error word (1 = wait ran out, 2 = a size exceeds the declared maxima)
+  int *err;    // scratch: error word (1 = wait ran out, 2 = inputs rejected by the validation)
   int *chain;  // scratch: ancestor ids per node, laid out like the labels
   long long spin_limit;
   int max_sep;
@@ -64,6 +67,45 @@ __device__ __forceinline__ int na_ld_relaxed(const int *p) {
   return v;
 }
 
+// Every access the fill makes is bounded by these checks: rows and position
+// lists lie inside [0, total_label) and are non-empty, ids are in [0, n),
+// a node's father is one level up (so its ancestor chain is exactly d-1
+// long), and a position list is sorted, ends with the node itself and names
+// proper ancestors at their own depths (so every label read stays inside the
+// row it reads).  Any violation sets the error word to 2.
+__global__ void __launch_bounds__(256) validate_noalloc_kernel(NoAllocArgs A) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    if (__ldg(A.dis_hash) < 0 || __ldg(A.dis_hash + A.n) > A.total_label || __ldg(A.pos_hash) < 0)
+      atomicCAS(A.err, 0, 2);
+  }
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < A.n; i += stride) {
+    const int v = (int)i;
+    bool ok = true;
+    const int o = __ldg(A.order + v);
+    ok &= o >= 0 && o < A.n;
+    const int d = __ldg(A.depth + v);
+    const int64_t r0 = __ldg(A.dis_hash + v), r1 = __ldg(A.dis_hash + v + 1);
+    ok &= d >= 1 && d <= A.max_depth && r0 >= 0 && r1 >= r0 && d <= r1 - r0;
+    const int f = __ldg(A.father + v);
+    if (f < 0) ok &= f == -1 && d == 1;
+    else ok &= f < A.n && __ldg(A.depth + f) == d - 1;
+    const int64_t p0 = __ldg(A.pos_hash + v), p1 = __ldg(A.pos_hash + v + 1);
+    const int64_t cnt = p1 - p0;
+    ok &= p0 >= 0 && cnt >= 1 && cnt - 1 <= A.max_sep;
+    if (ok) {
+      int prev = -1;
+      for (int64_t k = p0; k < p1 && ok; k++) {
+        const int u = __ldg(A.pos_id + k), p = __ldg(A.pos_pos + k);
+        ok &= u >= 0 && u < A.n && p > prev;
+        if (ok) ok &= (k == p1 - 1) ? (u == v && p == d - 1) : (p < d - 1 && __ldg(A.depth + u) == p + 1);
+        prev = p;
+      }
+    }
+    if (!ok) atomicCAS(A.err, 0, 2);
+  }
+}
+
 __global__ void __launch_bounds__(128) fill_noalloc_kernel(NoAllocArgs A) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ int s_t, s_stop;
@@ -72,7 +114,7 @@ __global__ void __launch_bounds__(128) fill_noalloc_kernel(NoAllocArgs A) {
   int64_t *anc_row = xs_row + A.max_sep;        // [max_depth]
   int *xs_p = (int *)(anc_row + A.max_depth);   // [max_sep]
   int *xs_w = xs_p + A.max_sep;                 // [max_sep]
-  if (tid == 0 && __ldg(A.dis_hash + A.n) > A.total_label) atomicCAS(A.err, 0, 2);
+  if (na_ld_relaxed(A.err) != 0) return;  // the inputs failed validation: write nothing
   for (;;) {
     if (tid == 0) s_t = atomicAdd(A.next, 1);
     __syncthreads();
@@ -85,8 +127,8 @@ __global__ void __launch_bounds__(128) fill_noalloc_kernel(NoAllocArgs A) {
     const int m = (int)(__ldg(A.pos_hash + v + 1) - pb) - 1;
     if (tid == 0) {
       s_stop = 0;
-      const bool row_fits = d <= __ldg(A.dis_hash + v + 1) - __ldg(A.dis_hash + v);
-      if (m > A.max_sep || d > A.max_depth || !row_fits || na_ld_relaxed(A.err) != 0) {
+      const bool row_fits = d >= 1 && d <= __ldg(A.dis_hash + v + 1) - __ldg(A.dis_hash + v);
+      if (m < 0 || m > A.max_sep || d > A.max_depth || !row_fits || na_ld_relaxed(A.err) != 0) {
         atomicCAS(A.err, 0, 2);
         s_stop = 1;
       } else if (f >= 0) {
@@ -219,6 +261,8 @@ extern "C" int h2h_fill_labels_l4_noalloc(int n, const int *order, const int *fa
   A.spin_limit = 4000000000LL;
   A.max_sep = max_sep;
   A.max_depth = max_depth;
+  const int vblocks = (int)std::min<int64_t>((int64_t)nsm * 4, ((int64_t)n + 255) / 256);
+  validate_noalloc_kernel<<<std::max(1, vblocks), 256, 0, s>>>(A);
   const int blocks = (int)std::min<int64_t>((int64_t)nsm * std::max(1, per_sm), n);
   fill_noalloc_kernel<<<std::max(1, blocks), 128, smem, s>>>(A);
   e = cudaGetLastError();
@@ -234,8 +278,9 @@ extern "C" int h2h_fill_labels_l4_noalloc(int n, const int *order, const int *fa
     return H2H_ERR_CUDA;
   }
   if (kerr != 0) {
-    set_last_error(kerr == 2 ? "h2h_fill_labels_l4_noalloc: a node exceeds max_depth/max_sep or dis_hash[n] > "
-                               "total_label"
+    set_last_error(kerr == 2 ? "h2h_fill_labels_l4_noalloc: inputs rejected before any write (an offset, id or "
+                               "depth is out of range, a father is not one level up, a position list is not "
+                               "sorted ending with its node, or a node exceeds max_depth/max_sep)"
                              : "h2h_fill_labels_l4_noalloc: a dependency wait ran out (order must list every "
                                "father before its children)");
     return H2H_ERR_DEVICE;

@@ -91,7 +91,9 @@ int h2h_query_nolca_nohub(const h2h_graph *g, int x, int y);
  * n pairs from device buffers x, y into device buffer out, enqueued on the
  * caller's cudaStream_t (NULL = legacy default stream); does not synchronize.
  * A pair with an id outside [0, n) answers -1 (the reference reads out of
- * bounds there).
+ * bounds there); this call does not report it otherwise, so a caller that
+ * cannot trust its ids checks the answers for -1.  Host batches and single
+ * pairs keep their own flag, so such a batch never fails a later call.
  * The reference wrappers return elapsed microseconds; time with events on
  * the same stream instead. */
 int h2h_query_batch(const h2h_graph *g, const int *x_dev, const int *y_dev, int *out_dev, int64_t n,
@@ -99,7 +101,9 @@ int h2h_query_batch(const h2h_graph *g, const int *x_dev, const int *y_dev, int 
 
 /* The same from host buffers: copies x, y to the device, runs the batch and
  * copies the answers back before returning (the Query_noHub flow,
- * main.cu:218-240: translateQuery, kernel, translateQueryResultBack). */
+ * main.cu:218-240: translateQuery, kernel, translateQueryResultBack).
+ * Returns H2H_ERR_ARG when a pair holds an id outside [0, n) (those pairs
+ * answer -1); the flag it reads belongs to this call path alone. */
 int h2h_query_batch_host(const h2h_graph *g, const int *x, const int *y, int *out, int64_t n, int mode);
 
 /* Sizes and per-phase times of a built index (the printConstructInfo columns,
@@ -138,20 +142,27 @@ int h2h_write_query_result(const h2h_graph *g, const char *root, int64_t query_n
 
 /* L4 label fill that allocates nothing.  No counterpart in the reference: it
  * is for callers that cannot call cudaMalloc -- code running inside another
- * framework's memory budget or capture region, or plugins that may only use
- * the buffers their host hands them.  Every input and the output `dis` are
- * caller-owned device buffers laid out as h2h_copy_tree / h2h_copy_bfs /
- * h2h_copy_labels return them (order = TreeBFS, any order that lists each
- * father before its children works; pos_w = shortcut weight of each pos
- * entry, 0 for the node itself; dis_hash has n+1 offsets and dis_hash[n] ==
- * total_label).  The fill's scratch lives in a fixed 32 MiB __device__ array
- * that every GPU loading the library holds until exit, so the call takes at
- * most n + total_label + 2 <= 8,388,608 (larger trees: H2H_ERR_ARG), and
+ * framework's device-memory budget, services whose device memory is
+ * partitioned up front, or plugins that may only use the buffers their host
+ * hands them.  Every input and the output `dis` are caller-owned device
+ * buffers laid out as h2h_copy_tree / h2h_copy_bfs / h2h_copy_labels return
+ * them (order = TreeBFS, any order that lists each father before its
+ * children works; pos_w = shortcut weight of each pos entry, 0 for the node
+ * itself; pos_id / pos_pos / pos_w hold pos_hash[n] entries, dis holds
+ * total_label).  A first pass checks every offset, id and depth (dis_hash
+ * and pos_hash non-decreasing within [0, total_label] / from 0, ids in
+ * [0, n), depth[father[v]] == depth[v] - 1, each position list sorted by
+ * position, ending with the node itself and naming ancestors at their own
+ * depths) and returns H2H_ERR_DEVICE with nothing written when one fails.
+ * The fill's scratch lives in a fixed 32 MiB __device__ array that every
+ * GPU loading the library holds until exit, so the call takes at most
+ * n + total_label + 2 <= 8,388,608 (larger trees: H2H_ERR_ARG), and
  * max_depth / max_sep (largest depth, largest |X(v)|-1) must fit the
  * shared-memory staging (16*max_sep + 8*max_depth bytes).  The first call on
  * a device looks up the array's device address (make it before any stream
  * capture).  All calls share the array: calls that overlap on the GPU race.
- * Runs on `stream` and waits for it before returning. */
+ * Runs on `stream` and synchronizes it before returning (the status is read
+ * back from the device). */
 int h2h_fill_labels_l4_noalloc(int n, const int *order, const int *father, const int *depth,
                                const int64_t *pos_hash, const int *pos_id, const int *pos_pos, const int *pos_w,
                                const int64_t *dis_hash, int64_t total_label, int *dis, int max_depth, int max_sep,

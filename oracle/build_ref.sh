@@ -1,7 +1,8 @@
 #!/usr/bin/env bash
 # build_ref.sh -- CPU-only build of the reference's own translation units
-# (test infrastructure).  Compiles the reference sources where they lie (REF,
-# default /root/reference) with g++ and Thrust's CPP device system, plus the
+# (test infrastructure).  Compiles the reference sources where they lie (REF;
+# this recipe is the one place that knows the default location of the
+# reference tree, /root/reference, in the build container) with g++ and Thrust's CPP device system, plus the
 # harness and stubs in this directory, into oracle/_ref/ (git-ignored):
 #
 #   oracle/_ref/ref_harness_L3   the reference as shipped (L3 labels)
@@ -18,7 +19,7 @@ HERE=$(cd "$(dirname "$0")" && pwd)
 OUT="$HERE/_ref"
 CUDA=${CUDA_HOME:-/usr/local/cuda}
 if [ ! -f "$REF/Graph_D.cuh" ]; then
-  echo "build_ref.sh: reference tree not found at $REF" >&2
+  echo "build_ref.sh: reference tree not found at $REF (nothing to build)" >&2
   exit 3
 fi
 mkdir -p "$OUT/src" "$OUT/obj"

@@ -970,3 +970,11 @@ void or_get_adj(const or_graph *g, int64_t *ah, int *aid, int *aw) {
   }
   ah[g->n] = t;
 }
+
+/* Input arcs in adjList order (file order, self loops dropped): off[n+1],
+ * v[m].  The local-pair generator walks them. */
+int64_t or_input_arcs(const or_graph *g) { return g->m; }
+void or_get_input_arcs(const or_graph *g, int *off, int *v) {
+  for (int i = 0; i <= g->n; i++) off[i] = g->adj_off[i];
+  for (int64_t e = 0; e < g->m; e++) v[e] = g->adj[e].v;
+}

@@ -81,6 +81,20 @@ void or_get_bfs(const or_graph *g, int *tree_bfs, int *tree_hash);
 int64_t or_adj_total(const or_graph *g);
 void or_get_adj(const or_graph *g, int64_t *adj_hash, int *adj_id, int *adj_w);
 
+/* Input arcs in the loader's adjList order (file order, self loops
+ * dropped): off receives n+1 offsets, v the or_input_arcs() targets. */
+int64_t or_input_arcs(const or_graph *g);
+void or_get_input_arcs(const or_graph *g, int *off, int *v);
+
+/* Workload generators (oracle/gen_shim.cpp over the library's generator
+ * source, so a CPU-only run draws the same graph and pairs without the GPU
+ * library).  Status 0 = ok; on error msg receives a message. */
+void or_gen_default(void *params /* h2h_gen_params: the 64x64 test grid */);
+int or_generate_road(const void *params /* h2h_gen_params, include/gpuh2h_tools.h */, const char *root, const char *name, int64_t *n_arcs,
+                     char *msg, int msg_len);
+int or_gen_uniform_pairs(int n_vertices, int64_t n, uint64_t seed, int *x, int *y);
+int or_gen_local_pairs(const or_graph *g, int64_t n, int max_hops, uint64_t seed, int *x, int *y);
+
 /* Restated per-cell body of makeCHPerHeight_D_2 (kernel_functions.cu:319-478)
  * on the reference's AoS arrays.  Exposed for the reference harness, which
  * substitutes it for the GPU launch in the CPU-only build.  Returns 0, or

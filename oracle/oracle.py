@@ -18,18 +18,45 @@ LIB = os.path.join(BUILD, "liboracle.so")
 REF_DIR = os.path.join(HERE, "_ref")
 
 
+PKG_CSRC = os.path.join(os.path.dirname(HERE), "gpu-h2h_gb300", "csrc")
+INCLUDE = os.path.join(os.path.dirname(HERE), "include")
+
+
 def build(force: bool = False) -> str:
-    """Compile h2h_oracle.c into oracle/_build/liboracle.so (gcc, plain C)."""
-    src = os.path.join(HERE, "h2h_oracle.c")
-    hdr = os.path.join(HERE, "h2h_oracle.h")
-    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= max(
-            os.path.getmtime(src), os.path.getmtime(hdr)):
+    """Compile oracle/_build/liboracle.so: h2h_oracle.c (gcc, plain C) plus
+    the workload generators (the library's gen.cpp and gen_shim.cpp, g++),
+    so a CPU-only run needs nothing from the GPU library."""
+    srcs = [os.path.join(HERE, "h2h_oracle.c"), os.path.join(HERE, "gen_shim.cpp"),
+            os.path.join(PKG_CSRC, "gen.cpp")]
+    deps = srcs + [os.path.join(HERE, "h2h_oracle.h"), os.path.join(PKG_CSRC, "gen.h"),
+                   os.path.join(PKG_CSRC, "status.h"), os.path.join(INCLUDE, "gpuh2h_tools.h"),
+                   os.path.join(INCLUDE, "gpuh2h.h")]
+    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= max(os.path.getmtime(d) for d in deps):
         return LIB
     os.makedirs(BUILD, exist_ok=True)
-    tmp = LIB + ".tmp%d" % os.getpid()
-    subprocess.check_call(["gcc", "-std=c11", "-O2", "-fPIC", "-shared", "-o", tmp, src, "-lpthread"])
+    inc = ["-I" + HERE, "-I" + PKG_CSRC, "-I" + INCLUDE]
+    tag = "%d" % os.getpid()
+    objs = [os.path.join(BUILD, os.path.basename(x) + "." + tag + ".o") for x in srcs]
+    procs = [subprocess.Popen(["gcc", "-std=c11", "-O2", "-fPIC", "-c", srcs[0], "-o", objs[0]])]
+    for src, obj in zip(srcs[1:], objs[1:]):
+        procs.append(subprocess.Popen(["g++", "-std=c++17", "-O2", "-fPIC", *inc, "-c", src, "-o", obj]))
+    if any(p.wait() != 0 for p in procs):
+        raise RuntimeError("oracle build failed")
+    tmp = LIB + ".tmp" + tag
+    subprocess.check_call(["g++", "-shared", "-o", tmp, *objs, "-lpthread"])
     os.replace(tmp, LIB)
+    for o in objs:
+        os.remove(o)
     return LIB
+
+
+class GenParams(C.Structure):
+    """h2h_gen_params (include/gpuh2h_tools.h)."""
+    _fields_ = [("n", C.c_int64), ("cols", C.c_int32), ("aspect_milli", C.c_int32), ("jitter_milli", C.c_int32),
+                ("drop_permille", C.c_int32), ("target_arcs", C.c_int64), ("diag_permille", C.c_int32),
+                ("hw_tiers", C.c_int32), ("hw_permille10", C.c_int32), ("hw_k", C.c_int32),
+                ("hw_scale_milli", C.c_int32), ("weight_max", C.c_int32), ("partition_height", C.c_int32),
+                ("seed", C.c_uint64)]
 
 
 _lib = None
@@ -64,6 +91,13 @@ def lib():
         L.or_get_labels.argtypes = [vp, vp, vp, vp, vp, vp]
         L.or_get_bfs.argtypes = [vp, vp, vp]
         L.or_get_adj.argtypes = [vp, vp, vp, vp]
+        L.or_input_arcs.argtypes = [vp]
+        L.or_input_arcs.restype = i64
+        L.or_get_input_arcs.argtypes = [vp, vp, vp]
+        L.or_gen_default.argtypes = [vp]
+        L.or_generate_road.argtypes = [vp, C.c_char_p, C.c_char_p, C.POINTER(i64), C.c_char_p, i32]
+        L.or_gen_uniform_pairs.argtypes = [i32, i64, C.c_uint64, vp, vp]
+        L.or_gen_local_pairs.argtypes = [vp, i64, i32, C.c_uint64, vp, vp]
         _lib = L
     return _lib
 
@@ -170,6 +204,21 @@ class OracleGraph:
                                threads or self.threads)
         return out
 
+    def local_pairs(self, n: int, max_hops: int = 20, seed: int = 1):
+        """The library's local-pair generator over this graph's input arcs."""
+        x = np.empty(n, np.int32)
+        y = np.empty(n, np.int32)
+        if self._L.or_gen_local_pairs(self.h, n, max_hops, seed, _p(x), _p(y)) != 0:
+            raise ValueError("bad local-pair arguments")
+        return x, y
+
+    def input_arcs(self):
+        n = self.n
+        off = np.empty(n + 1, np.int32)
+        v = np.empty(self._L.or_input_arcs(self.h), np.int32)
+        self._L.or_get_input_arcs(self.h, _p(off), _p(v))
+        return off, v
+
     def dijkstra(self, src: int):
         d = np.empty(self.n, np.int32)
         self._L.or_dijkstra(self.h, int(src), _p(d))
@@ -181,6 +230,30 @@ class OracleGraph:
                     label_size=L.or_label_size(self.h), pos_size=L.or_pos_size(self.h),
                     rmq_size=L.or_rmq_size(self.h), lub=L.or_lub_size(self.h),
                     gpu_vertices=L.or_gpu_vertices(self.h), levels=L.or_n_levels(self.h))
+
+
+def generate_road(root: str, name: str, **kw) -> int:
+    """The library's seeded road-graph generator (same bytes as
+    gpuh2h.generate_road); returns the arc count."""
+    L = lib()
+    p = GenParams()
+    L.or_gen_default(C.byref(p))
+    for k, v in kw.items():
+        setattr(p, k, v)
+    arcs = C.c_int64()
+    msg = C.create_string_buffer(512)
+    rc = L.or_generate_road(C.byref(p), root.encode(), name.encode(), C.byref(arcs), msg, 512)
+    if rc != 0:
+        raise RuntimeError("generator: %s" % msg.value.decode())
+    return arcs.value
+
+
+def uniform_pairs(n_vertices: int, n: int, seed: int = 1):
+    x = np.empty(n, np.int32)
+    y = np.empty(n, np.int32)
+    if lib().or_gen_uniform_pairs(n_vertices, n, seed, _p(x), _p(y)) != 0:
+        raise ValueError("bad pair arguments")
+    return x, y
 
 
 def run_reference(edge, idf, cut, H, Cg, threads=4, l4=True, pairs=None):

@@ -11,8 +11,8 @@ Large arrays of the 64x64 case are stored as SHA-256 digests plus samples.
 It also checks that the C oracle (oracle/h2h_oracle.c) reproduces every
 array, so the fixtures pin both.
 
-Usage (needs the reference tree, i.e. only in the build container):
-    python tests/golden/make_golden.py [--ref /root/reference]
+Usage (needs the reference tree; REF or --ref names it):
+    REF=<reference tree> python tests/golden/make_golden.py
 """
 from __future__ import annotations
 
@@ -62,8 +62,10 @@ def compare(ref: dict, orc: dict, what: str):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("REF"), help="the reference tree (default: $REF)")
     args = ap.parse_args()
+    if not args.ref:
+        raise SystemExit("make_golden.py: name the reference tree with --ref or REF")
     env = dict(os.environ, REF=args.ref)
     subprocess.check_call([os.path.join(REPO, "oracle", "build_ref.sh")], env=env)
     # 13-vertex sample: copy the input files next to the fixtures

@@ -148,6 +148,32 @@ def test_generators_are_seeded_and_in_range(cfg0_root):
         assert int(t) in seen
 
 
+def test_oracle_generators_equal_library_generators(tmp_path):
+    """The CPU baseline draws its graph and pairs through the oracle library
+    (no GPU library in that process): same files, same uniform and local
+    pairs as the library's generators."""
+    import gpuh2h
+    from oracle import oracle
+    kw = dict(n=20000, target_arcs=55000, aspect_milli=1300, jitter_milli=300, diag_permille=50, hw_tiers=2,
+              hw_permille10=50, hw_k=3, hw_scale_milli=400, partition_height=7, seed=11, cols=0, drop_permille=0)
+    a, b = str(tmp_path / "lib"), str(tmp_path / "ora")
+    assert gpuh2h.generate_road(a, "w", **kw) == oracle.generate_road(b, "w", **kw)
+    for fa, fb in zip(gpuh2h.files_for(a, "w"), gpuh2h.files_for(b, "w")):
+        assert open(fa, "rb").read() == open(fb, "rb").read(), fa
+    for u, v in zip(gpuh2h.uniform_pairs(20000, 5000, 3), oracle.uniform_pairs(20000, 5000, 3)):
+        assert np.array_equal(u, v)
+    files = gpuh2h.files_for(a, "w")
+    g = gpuh2h.Graph("w", 7, 2, 2, 1, files=files)
+    o = oracle.OracleGraph(*files, 7, 2, 2)
+    for u, v in zip(g.local_pairs(5000, 20, 5), o.local_pairs(5000, 20, 5)):
+        assert np.array_equal(u, v)
+    off, v, _ = g.input_arcs()
+    off2, v2 = o.input_arcs()
+    assert np.array_equal(off, off2) and np.array_equal(v, v2)
+    g.close()
+    o.close()
+
+
 def test_g2h_cli_argument_count_rule(tmp_path):
     from gpuh2h import _build
     _build.build()

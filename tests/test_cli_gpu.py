@@ -7,6 +7,22 @@ import pytest
 
 pytestmark = pytest.mark.gpu
 
+# The reference's CSV header lines, byte for byte: contract.csv and
+# constructInfo.csv share one header (TreeStructure.cu:77,
+# Graph_Fundamental.cu:148, with its two empty columns), random.csv has the
+# query-timing header (Query.cu:608).
+CONSTRUCT_HEADER = (
+    "graphName,PartitionTreeHeight,changeHeight,ParititionTime,makePartitionRankTreeTime,AlllocateLUBTime,LUBSize,"
+    "translateLUBToGPUTime,TDInGPUTime,translateBackAndMallocToCPUTime,vertexesConstructedInGPU,"
+    "DecompositionTreeSize,TDInCPUTime,TDTREEHeight,,RMQsize,translateRMQTime,H2HLabelSize,,"
+    "changeConstructDeviceSize,H2HmallocTime,H2HConstructBFSTreeTime,H2HTranslateBFSTreeTime,H2HUsingTime_CPU,"
+    "H2HTranslateTime,H2HUsingTime_GPU,PartitionMethod,threadNum,contractDevice,parallelFine,constructDevice")
+QUERY_HEADER = (
+    "queryNumber,sequence,multiThread-4,multiThread-6,multiThread-8,multiThread-10,multiThread-12,multiThread-14,"
+    "multiThread-16,GPUnoLCA-64,GPUwithLCA-64,GPUnoLCA-128,GPUwithLCA-128,GPUnoLCA-256,GPUwithLCA-256,"
+    "GPUnoLCA-512,GPUwithLCA-512,GPUnoLCA-1024,GPUwithLCA-1024,TreeHeight,changeHeight,PartitionMethod,"
+    "contractDevice")
+
 
 @pytest.mark.parametrize("label", ["L4", "L3"])
 def test_g2h_runs_and_writes_csvs(tmp_path, label):
@@ -27,10 +43,14 @@ def test_g2h_runs_and_writes_csvs(tmp_path, label):
     assert r.returncode == 0, r.stderr.decode()
     out = r.stdout.decode()
     assert "connect!" in out and "n=4096" in out
-    for f in ("ConstructInfo/cfg0/contract.csv", "ConstructInfo/cfg0/constructInfo.csv", "QueryResult/cfg0/random.csv"):
+    for f, header in (("ConstructInfo/cfg0/contract.csv", CONSTRUCT_HEADER),
+                      ("ConstructInfo/cfg0/constructInfo.csv", CONSTRUCT_HEADER),
+                      ("QueryResult/cfg0/random.csv", QUERY_HEADER)):
         p = os.path.join(root, f)
         assert os.path.exists(p), f
-        lines = open(p).read().strip().split("\n")
+        raw = open(p, "rb").read()
+        assert raw.startswith((header + "\n").encode()), f   # the header line, byte for byte
+        lines = raw.decode().strip().split("\n")
         assert len(lines) >= 2, f                 # header + one row
         assert len(lines[1].split(",")) == len(lines[0].split(",")), f
     assert any(f.endswith("PartitionRate.csv") for f in os.listdir(root))

@@ -1,6 +1,9 @@
 """The built index on disk: a handle read back with h2h_load_index answers
 every query and serves every accessor exactly like the handle that was
-saved (single build and a batch graph); a damaged file is refused."""
+saved (single build and a batch graph) and like the reference's golden
+outputs for the same graph; a damaged file is refused."""
+import hashlib
+
 import numpy as np
 import pytest
 
@@ -31,7 +34,25 @@ def _check_same(a, b, tmp_path):
         assert ia[k] == ib[k], k
 
 
-def test_save_load_single(cfg0_root, tmp_path):
+def _sha(a):
+    return np.frombuffer(hashlib.sha256(np.ascontiguousarray(a).tobytes()).digest(), np.uint8)
+
+
+def _check_golden(h, golden0, tag):
+    """The loaded handle against the reference's own outputs (C = 2, L4)."""
+    import gpuh2h
+    A = _all(h)
+    for k in ("order", "father", "depth", "first", "tree_hash"):
+        assert np.array_equal(A[k], golden0[tag + k]), k
+    for k in ("rmq_hash", "rmq_id", "dis_hash", "dis", "pos_hash", "pos_id", "pos_pos", "tree_bfs", "adj_hash",
+              "adj_id", "adj_w"):
+        assert np.array_equal(_sha(A[k]), golden0[tag + "sha256/" + k]), k
+    pairs = golden0["pairs"]
+    assert np.array_equal(h.query(pairs[:, 0], pairs[:, 1], gpuh2h.QUERY_LCA), golden0[tag + "q_lca"])
+    assert np.array_equal(h.query(pairs[:, 0], pairs[:, 1], gpuh2h.QUERY_NOLCA), golden0[tag + "q_nolca"])
+
+
+def test_save_load_single(cfg0_root, golden0, tmp_path):
     import gpuh2h
     g = gpuh2h.Graph("cfg0", 6, 2, 4, 1, files=gpuh2h.files_for(cfg0_root, "cfg0"))
     g.contraction_noHub(1).constructLabel_noHub(2, 1, gpuh2h.LABEL_L4)
@@ -39,6 +60,7 @@ def test_save_load_single(cfg0_root, tmp_path):
     g.save_index(p)
     h = gpuh2h.Graph.load_index(p)
     _check_same(g, h, tmp_path)
+    _check_golden(h, golden0, "cfg0_C2_L4/")
     with pytest.raises(gpuh2h.H2HError):
         h.local_pairs(10)                 # no input arcs in a loaded index
     # a damaged position list is refused
@@ -56,7 +78,7 @@ def test_save_load_single(cfg0_root, tmp_path):
     h.close()
 
 
-def test_save_load_batch_graph(cfg0_root, tmp_path):
+def test_save_load_batch_graph(cfg0_root, golden0, tmp_path):
     import gpuh2h
     from conftest import sample13_files
     gs = [gpuh2h.Graph("s", 4, 1, 2, 1, files=sample13_files("Latitude")),
@@ -66,6 +88,7 @@ def test_save_load_batch_graph(cfg0_root, tmp_path):
     gs[1].save_index(p)
     h = gpuh2h.Graph.load_index(p)
     _check_same(gs[1], h, tmp_path)
+    _check_golden(h, golden0, "cfg0_C2_L4/")
     h.close()
     b.close()
     for g in gs:

@@ -117,6 +117,33 @@ def test_query_edge_cases(cfg0_root, golden0):
     assert np.array_equal(a, b)
 
 
+def test_bad_device_batch_does_not_fail_later_host_calls(cfg0_root, golden0):
+    """A device-buffer batch with an out-of-range id answers -1 for that pair;
+    a clean host batch and a single-pair query on the same graph afterwards
+    succeed (the host path has its own flag)."""
+    import torch
+
+    import gpuh2h
+    g = build(gpuh2h.files_for(cfg0_root, "cfg0"), 6, 1)
+    x = torch.tensor([0, 5, 9], dtype=torch.int32, device="cuda")
+    y = torch.tensor([7, 4096, 3], dtype=torch.int32, device="cuda")
+    out = torch.empty_like(x)
+    g.query_device(x.data_ptr(), y.data_ptr(), out.data_ptr(), 3, gpuh2h.QUERY_LCA,
+                   torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    assert out[1].item() == -1 and out[0].item() >= 0
+    pairs = golden0["pairs"]
+    tag = "cfg0_C1_L4/"
+    assert np.array_equal(g.query(pairs[:, 0], pairs[:, 1], gpuh2h.QUERY_LCA), golden0[tag + "q_lca"])
+    a, b = int(pairs[3, 0]), int(pairs[3, 1])
+    assert g.H2HDistancQuery_UsingLCA_noHub(a, b) == golden0[tag + "q_lca"][3]
+    # a bad host batch fails once, and the next clean one succeeds
+    with pytest.raises(gpuh2h.H2HError):
+        g.query(np.array([1], np.int32), np.array([-2], np.int32))
+    assert np.array_equal(g.query(pairs[:, 0], pairs[:, 1], gpuh2h.QUERY_NOLCA), golden0[tag + "q_nolca"])
+    g.close()
+
+
 def test_device_batch_on_caller_stream(cfg0_root, golden0):
     import torch
 
