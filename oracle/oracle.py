@@ -256,10 +256,31 @@ def uniform_pairs(n_vertices: int, n: int, seed: int = 1):
     return x, y
 
 
-def run_reference(edge, idf, cut, H, Cg, threads=4, l4=True, pairs=None):
-    """Run the CPU build of the reference (oracle/_ref, built by build_ref.sh)
-    and return its dumped arrays.  Only available where that build exists."""
-    exe = os.path.join(REF_DIR, "ref_harness_L4" if l4 else "ref_harness_L3")
+def build_ref_gpu() -> bool:
+    """Build the reference's own GPU code (oracle/build_ref_gpu.sh --build)
+    from the staged sources; False where nothing was staged."""
+    rc = subprocess.call([os.path.join(HERE, "build_ref_gpu.sh"), "--build"], stdout=subprocess.DEVNULL)
+    if rc == 3:
+        return False
+    if rc != 0:
+        raise RuntimeError("build_ref_gpu.sh --build failed (exit %d)" % rc)
+    return True
+
+
+def run_reference(edge, idf, cut, H, Cg, threads=4, l4=True, pairs=None, gpu=False):
+    """Run a build of the reference and return its dumped arrays.
+
+    gpu=False: the CPU build (oracle/_ref/ref_harness_L{3,4}, build_ref.sh).
+    gpu=True: the reference's own GPU kernels built for sm_103a
+    (oracle/_ref/ref_gpu_harness_L4, build_ref_gpu.sh): GPU partition
+    contraction, GPU LL label fill with the L4 walk, GPU batched queries;
+    its phase timers come back under "times" (microseconds)."""
+    if gpu:
+        if not l4:
+            raise ValueError("the GPU harness is built with the L4 label kernel only")
+        exe = os.path.join(REF_DIR, "ref_gpu_harness_L4")
+    else:
+        exe = os.path.join(REF_DIR, "ref_harness_L4" if l4 else "ref_harness_L3")
     if not os.path.exists(exe):
         raise FileNotFoundError(exe)
     with tempfile.TemporaryDirectory() as wd:
@@ -271,9 +292,13 @@ def run_reference(edge, idf, cut, H, Cg, threads=4, l4=True, pairs=None):
             pf = os.path.join(wd, "pairs.i32")
             np.ascontiguousarray(pairs, np.int32).tofile(pf)
             args.append(pf)
-        subprocess.run(args, cwd=wd, check=True, stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+        subprocess.run(args, cwd=wd, check=True, stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL,
+                       timeout=600)
         res = {}
         for f in os.listdir(out):
             name, ext = f.rsplit(".", 1)
-            res[name] = np.fromfile(os.path.join(out, f), dtype=np.int32 if ext == "i32" else np.int64)
+            if ext == "txt":
+                res[name] = {k: int(v) for k, v in (line.split() for line in open(os.path.join(out, f)) if line.strip())}
+            else:
+                res[name] = np.fromfile(os.path.join(out, f), dtype=np.int32 if ext == "i32" else np.int64)
         return res
