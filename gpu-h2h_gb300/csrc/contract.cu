@@ -144,6 +144,13 @@ __device__ __forceinline__ NbrMeta load_meta(const ElimArgs &A, int u) {
 //   P = valid entries of u's list except v (kernel_functions.cu:364-390),
 //   output = P with the first entry of every matched id min-updated, plus the
 //   unmatched members of Q inserted in order (:392-457).
+//
+// kWide: the list is read with 128-bit loads, four per lane in flight (2 KB
+// of ids and 2 KB of weights per warp per round trip instead of 512 B each):
+// near the top of the order lists hold thousands of entries and the load is
+// the merge's latency.  The slot arrays are padded by four entries, so a
+// vector that starts inside the list never leaves the allocation.
+template <bool kWide>
 __device__ void merge_neighbour(const ElimArgs &A, int u, const NbrMeta &m, int wu, int iu, int v, int hnow,
                                 const int *aid, const int *aw, int c, int *pid, int *pw, int lane, Cand cand,
                                 int nslots) {
@@ -151,8 +158,53 @@ __device__ void merge_neighbour(const ElimArgs &A, int u, const NbrMeta &m, int 
   const int s = m.s;
   const int J = m.J;
   int np = 0;
+  if (kWide) {
+    const int64_t lo = off + J, hi = off + s;
+    for (int64_t base = lo & ~int64_t(3); base < hi; base += 4 * 32 * 4) {
+      int4 xv[4], wv[4];
+#pragma unroll
+      for (int r = 0; r < 4; r++) {
+        const int64_t e = base + (int64_t)(r * 32 + lane) * 4;
+        if (e < hi) {
+          xv[r] = __ldcg(reinterpret_cast<const int4 *>(A.slot_nbr + e));
+          wv[r] = __ldcg(reinterpret_cast<const int4 *>(A.slot_w + e));
+        } else {
+          xv[r] = make_int4(v, v, v, v);
+          wv[r] = make_int4(0, 0, 0, 0);
+        }
+      }
+#pragma unroll
+      for (int r = 0; r < 4; r++) {
+        const int64_t e = base + (int64_t)(r * 32 + lane) * 4;
+        const int xs[4] = {xv[r].x, xv[r].y, xv[r].z, xv[r].w};
+        const int ws[4] = {wv[r].x, wv[r].y, wv[r].z, wv[r].w};
+        bool keep[4];
+        int kc = 0;
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+          keep[k] = e + k >= lo && e + k < hi && xs[k] != v;
+          kc += keep[k];
+        }
+        int incl = kc;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const int y = __shfl_up_sync(0xffffffffu, incl, o);
+          if (lane >= o) incl += y;
+        }
+        int pos = np + incl - kc;
+#pragma unroll
+        for (int k = 0; k < 4; k++)
+          if (keep[k]) {
+            pid[pos] = xs[k];
+            pw[pos] = ws[k];
+            pos++;
+          }
+        np += __shfl_sync(0xffffffffu, incl, 31);
+      }
+    }
+  }
   // u's list minus v, loaded four warp-widths at a time so the L2 round trips overlap
-  for (int base = J; base < s; base += 128) {
+  for (int base = J; !kWide && base < s; base += 128) {
     int x[4], w[4];
 #pragma unroll
     for (int r = 0; r < 4; r++) {
@@ -432,7 +484,7 @@ __global__ void __maxnreg__(48) elim_kernel(ElimArgs A) {
           if (lane == 0) set_err(A.err, kErrStaging);
           continue;
         }
-        merge_neighbour(A, u, m, aw[i], i, v, hnow, aid, aw, c, pid, pw, lane, lead, k);
+        merge_neighbour<false>(A, u, m, aw[i], i, v, hnow, aid, aw, c, pid, pw, lane, lead, k);
       }
     }
     cluster.sync();  // no CTA leaves while a peer may still read the leader's shared memory
@@ -710,7 +762,7 @@ __global__ void __launch_bounds__(512, 1) cell_grid_kernel(GridArgs H) {
         if (lane == 0) set_err(A.err, kErrStaging);
         continue;
       }
-      merge_neighbour(A, u, m, aw[i], i, v, hnow, aid, aw, c, pid, pw, lane, cand, ns);
+      merge_neighbour<true>(A, u, m, aw[i], i, v, hnow, aid, aw, c, pid, pw, lane, cand, ns);
     }
     __syncthreads();
     // ---- after the first pick of a partition cell every key becomes live
@@ -895,6 +947,14 @@ ElimPlan::ElimPlan(const std::vector<Graph *> &graphs) : gs(graphs) {
   const int K = (int)gs.size();
   GH_CHECK(K >= 1, H2H_ERR_ARG, "no graph to contract");
   const bool force_global_stage = std::getenv("GPUH2H_GLOBAL_STAGING") != nullptr;
+  // cooperative steps keep merge buffers in shared memory only when this
+  // many warps' buffers fit, else 16 warps with buffers in global memory
+  // (GPUH2H_GRID_SMEM_WARPS; 17 = always global).  Measured on the
+  // 6.26M-vertex graph: lists of 3,456-4,264 entries left room for 5-6
+  // warps, and 16 warps staging in global memory took those levels from
+  // 212 + 480 to 194 + 403 ms; at 8 warps and above shared memory wins.
+  int grid_smem_warps = 8;
+  if (const char *e = std::getenv("GPUH2H_GRID_SMEM_WARPS")) grid_smem_warps = std::max(1, std::atoi(e));
   // cell list bounds come with the elimination sets (build_elimination_sets)
   std::vector<GraphLevels> L(K);
   int threads = 1;
@@ -1060,11 +1120,12 @@ ElimPlan::ElimPlan(const std::vector<Graph *> &graphs) : gs(graphs) {
     }
     const int64_t own = 3 * al(4LL * lmax) + 4 * al(4LL * slice_max), per_warp = 2 * al(4LL * lmax);
     if (own > smem_dyn_g) return false;
-    // per-warp merge buffers in shared memory when 4+ warps' worth fit (a
-    // merge walks them serially), else 16 warps with buffers in global memory
+    // per-warp merge buffers in shared memory when grid_smem_warps+ warps'
+    // worth fit (a merge walks them serially), else 16 warps with buffers in
+    // global memory
     const int64_t fit = (smem_dyn_g - own) / per_warp;
-    const int hw = fit >= 4 ? (int)std::min<int64_t>(16, fit) : 16;
-    const bool gstage = fit < 4;
+    const int hw = fit >= grid_smem_warps ? (int)std::min<int64_t>(16, fit) : 16;
+    const bool gstage = fit < grid_smem_warps;
     const int64_t hsmem = gstage ? own : own + hw * per_warp;
     int per = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, cell_grid_kernel, hw * 32, (size_t)hsmem) !=
@@ -1201,8 +1262,8 @@ ElimPlan::ElimPlan(const std::vector<Graph *> &graphs) : gs(graphs) {
   }
   // ---- device state
   try {
-    slot_nbr = palloc<int>(pool_size, bytes);
-    slot_w = palloc<int>(pool_size, bytes);
+    slot_nbr = palloc<int>(pool_size + 4, bytes);  // + 4: a list's last 128-bit load stays inside
+    slot_w = palloc<int>(pool_size + 4, bytes);
     pool_next = palloc<unsigned long long>(1, bytes);
     pool_first = palloc<unsigned long long>(1, bytes);
     slot_off = palloc<int64_t>(N, bytes);

@@ -113,6 +113,7 @@ struct Graph {
   std::vector<int> hld, htop, hpos;
   std::vector<int64_t> seg_off;
   int max_segs = 0;
+  bool tree_layout = false;  // depth, first, level order, heavy paths, segments and dis_hash built on the GPU
   bool labelled = false;
   int64_t max_label = 0;
   // device
@@ -224,11 +225,13 @@ struct FillPlan {
   int *depth = nullptr, *dis = nullptr;
   // workspace
   int *hld = nullptr, *htop = nullptr, *hpos = nullptr, *seg_top = nullptr, *seg_pos = nullptr;
+  int64_t *hld_row = nullptr;
   int64_t *seg_off = nullptr;
   int *done = nullptr, *next = nullptr, *err = nullptr, *tiles = nullptr;
   unsigned long long *trace_t = nullptr;  // publish time per node (GPUH2H_TRACE)
   int64_t ntiles = 0, tiles_cap = 0, nchunks = 0;
   int max_u = 1, max_c = 1, max_segs = 1, blocks = 1, threads = 128;
+  int scalar_cols = 32;  // tiles this narrow sweep one column per lane (labels.cu)
   size_t smem = 0;
   int nsm = 0;
   int64_t work_bytes = 0;
@@ -257,12 +260,15 @@ void build_elimination_sets(const std::vector<Graph *> &gs);
 // fills g.elim (elimination order) and g.x_off / x_id / x_w
 void contract_gpu(Graph &g);
 void build_tree(Graph &g);                             // tree.cpp: father, children, Euler tour
+// tree_gpu.cu: the same on the GPU, plus the level order, heavy paths and
+// root-path segment offsets (sets g.tree_layout)
+void build_tree_gpu(Graph &g);
 // query.cu: the compacted sparse tables of the graphs' Euler tours on the
 // GPU (first, rmq_hash, rmq_id in each graph's DeviceIndex)
 void build_rmq_gpu(const std::vector<Graph *> &gs);
 void download_rmq(const Graph &g, int64_t *rmq_hash, int *rmq_id);  // query.cu
 inline void build_tree_and_rmq(Graph &g) {
-  build_tree(g);
+  build_tree_gpu(g);
   build_rmq_gpu({&g});
 }
 void allocate_labels_and_bfs(Graph &g);                // tree.cpp

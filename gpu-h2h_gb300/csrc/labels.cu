@@ -217,7 +217,7 @@ struct FlowArgs {
   const int *pos_id;
   const int *pos_pos;
   const int *pos_w;
-  const int *hld;          // heavy paths, top to bottom
+  const int64_t *hld_row;  // heavy paths, top to bottom: the row offset of the node at each position
   const int64_t *seg_off;  // root-path segments per node
   const int *seg_top, *seg_pos;
   int *done;          // per vertex: 1 once its row is visible
@@ -226,6 +226,7 @@ struct FlowArgs {
   long long spin_limit;
   int max_u;          // max separator members in one tile (staging size)
   int max_segs;       // max root-path segments of a node (staging size)
+  int scalar_cols;    // tiles of at most this many columns sweep one column per lane
   unsigned long long *trace_t;  // non-null (GPUH2H_TRACE): each node's publish time, ns
 };
 
@@ -311,28 +312,133 @@ __global__ void __launch_bounds__(128) fill_flow_kernel(FlowArgs A) {
     stop = __shfl_sync(0xffffffffu, stop, 0);
     __syncwarp();
     if (stop) return;
+    // Column sweep, four consecutive columns [J, J + 4) per lane (rows start
+    // on 16-byte boundaries and column blocks are multiples of four, so J is
+    // a multiple of four inside every row).  The tile's members are sorted by
+    // position, so for a lane's columns they fall into three runs:
+    //   i >= hi  (p >= J + 4): every column lies above u_i -- one 128-bit
+    //            load of u_i's row gives all four candidates;
+    //   i <  lo  (p <  J):     every column lies below u_i -- the candidate
+    //            of column j is the ancestor a_j's entry at p (L4);
+    //   lo <= i < hi:          at most four members with p inside the quad,
+    //            resolved column by column.
+    // No per-member branch, and a quarter of the iterations of a
+    // column-per-lane sweep.  A tile of 33 to 127 columns spreads its
+    // members over 2 or 4 lane groups (every group takes every G-th member)
+    // and combines the groups' minima with shuffles, so all 32 lanes work.
     const int cend = min(c1, d - 1);
-    for (int j = c0 + lane; j < cend; j += 32) {
-      // ancestor at depth j + 1: last segment whose top depth is <= j + 1
-      int lo = 0, hi = ns - 1;
-      while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if (s_top[mid] <= j + 1) lo = mid; else hi = mid - 1;
-      }
-      const int a = __ldg(A.hld + s_pos[lo] + (j + 1 - s_top[lo]));
-      const int64_t arow = __ldg(A.drow + a);
-      int r = INT_MAX;
+    if (cend - c0 <= A.scalar_cols) {
+      // a tile of at most scalar_cols columns (32 on trees of up to 2,048
+      // levels, whose narrow levels are a latency chain): one column per
+      // lane, one ancestor lookup each -- the shortest chain of dependent
+      // loads per tile
+      const int j = c0 + lane;
+      if (j < cend) {
+        int lo = 0, hi = ns - 1;
+        while (lo < hi) {
+          const int mid = (lo + hi + 1) >> 1;
+          if (s_top[mid] <= j + 1) lo = mid; else hi = mid - 1;
+        }
+        const int64_t arow = __ldg(A.hld_row + s_pos[lo] + (j + 1 - s_top[lo]));
+        int r = INT_MAX;
 #pragma unroll 8
-      for (int i = 0; i < nu; i++) {
-        const int p = xs_p[i];
-        int val;
-        if (p > j) val = __ldcg(A.dis + xs_row[i] + j);
-        else if (p == j) val = 0;
-        else val = __ldcg(A.dis + arow + p);
-        r = min(r, xs_w[i] + val);
+        for (int i = 0; i < nu; i++) {
+          const int p = xs_p[i];
+          const int val = p > j ? __ldcg(A.dis + xs_row[i] + j) : p == j ? 0 : __ldcg(A.dis + arow + p);
+          r = min(r, xs_w[i] + val);
+        }
+        if (whole_sep) A.dis[base + j] = r;
+        else atomicMin(A.dis + base + j, r);
       }
-      if (whole_sep) A.dis[base + j] = r;
-      else atomicMin(A.dis + base + j, r);
+    }
+    const int nquad = cend - c0 <= A.scalar_cols ? 0 : (cend - c0 + 3) >> 2;
+    const int QW = nquad > 16 ? 32 : nquad > 8 ? 16 : 8;  // lanes along the columns
+    const int G = 32 / QW;                                 // member groups
+    const int qi = lane & (QW - 1), grp = lane / QW;
+    for (int Jb = c0; nquad > 0 && Jb < cend; Jb += 4 * QW) {  // the same trip count in every lane
+      const int J = Jb + 4 * qi;
+      const bool active = J < cend;
+      const int nvalid = active ? min(4, cend - J) : 0;
+      int r0 = INT_MAX, r1 = INT_MAX, r2 = INT_MAX, r3 = INT_MAX;
+      if (active) {
+        int64_t arow[4];
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+          // ancestor at depth j + 1 (a column past cend reuses column J's
+          // ancestor: its reads stay inside that row or its padding and its
+          // result is discarded)
+          const int j = J + (k < nvalid ? k : 0);
+          int lo = 0, hi = ns - 1;
+          while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (s_top[mid] <= j + 1) lo = mid; else hi = mid - 1;
+          }
+          arow[k] = __ldg(A.hld_row + s_pos[lo] + (j + 1 - s_top[lo]));
+        }
+        int ilo = 0, ihi = nu;  // first member with p >= J
+        while (ilo < ihi) {
+          const int mid = (ilo + ihi) >> 1;
+          if (xs_p[mid] < J) ilo = mid + 1; else ihi = mid;
+        }
+        const int mlo = ilo;
+        ihi = nu;               // first member with p >= J + 4
+        while (ilo < ihi) {
+          const int mid = (ilo + ihi) >> 1;
+          if (xs_p[mid] < J + 4) ilo = mid + 1; else ihi = mid;
+        }
+        const int mhi = ilo;
+#pragma unroll 4
+        for (int i = mhi + grp; i < nu; i += G) {
+          const int4 x = __ldcg(reinterpret_cast<const int4 *>(A.dis + xs_row[i] + J));
+          const int w = xs_w[i];
+          r0 = min(r0, w + x.x);
+          r1 = min(r1, w + x.y);
+          r2 = min(r2, w + x.z);
+          r3 = min(r3, w + x.w);
+        }
+#pragma unroll 4
+        for (int i = grp; i < mlo; i += G) {
+          const int p = xs_p[i], w = xs_w[i];
+          r0 = min(r0, w + __ldcg(A.dis + arow[0] + p));
+          r1 = min(r1, w + __ldcg(A.dis + arow[1] + p));
+          r2 = min(r2, w + __ldcg(A.dis + arow[2] + p));
+          r3 = min(r3, w + __ldcg(A.dis + arow[3] + p));
+        }
+        for (int i = mlo + grp; i < mhi; i += G) {
+          const int p = xs_p[i], w = xs_w[i];
+          const int64_t ur = xs_row[i];
+          int c[4];
+#pragma unroll
+          for (int k = 0; k < 4; k++) {
+            const int j = J + k;
+            c[k] = p > j ? __ldcg(A.dis + ur + j) : p == j ? 0 : __ldcg(A.dis + arow[k] + p);
+          }
+          r0 = min(r0, w + c[0]);
+          r1 = min(r1, w + c[1]);
+          r2 = min(r2, w + c[2]);
+          r3 = min(r3, w + c[3]);
+        }
+      }
+      for (int o = QW; o < 32; o <<= 1) {  // combine the member groups (lanes qi, qi + QW, ...)
+        r0 = min(r0, __shfl_xor_sync(0xffffffffu, r0, o));
+        r1 = min(r1, __shfl_xor_sync(0xffffffffu, r1, o));
+        r2 = min(r2, __shfl_xor_sync(0xffffffffu, r2, o));
+        r3 = min(r3, __shfl_xor_sync(0xffffffffu, r3, o));
+      }
+      if (active && grp == 0) {
+        int *out = A.dis + base + J;
+        if (whole_sep && nvalid == 4) {
+          *reinterpret_cast<int4 *>(out) = make_int4(r0, r1, r2, r3);
+        } else {
+          const int r[4] = {r0, r1, r2, r3};
+#pragma unroll
+          for (int k = 0; k < 4; k++)
+            if (k < nvalid) {
+              if (whole_sep) out[k] = r[k];
+              else atomicMin(out + k, r[k]);
+            }
+        }
+      }
     }
     __syncwarp();
     if (lane == 0) {
@@ -442,6 +548,12 @@ __global__ void expand_tiles_kernel(const int *node_first, const int *node_ntile
     const int f = node_first[v], c = node_ntiles[v];
     for (int k = lane; k < c; k += 32) tile_node[f + k] = (int)v;
   }
+}
+
+// Row offset of the node at every heavy-path position (the fill reads an
+// ancestor's row offset with one load instead of two dependent ones).
+__global__ void hld_row_kernel(const int *hld, const int64_t *drow, int64_t *hld_row, int n) {
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) hld_row[k] = drow[hld[k]];
 }
 
 // Root-path segments of every node, shallowest first: walking up from v,
@@ -692,6 +804,17 @@ FillPlan::FillPlan(const std::vector<Graph *> &graphs, const TilePolicy &pol, co
   });
   f_drow[N] = dis_total;
   f_pos_hash[N] = pos_total;
+  // Narrow tiles sweep one column per lane on trees of up to 2,048 levels,
+  // whose narrow levels fill as a latency chain (264k-vertex graph: 29 ms
+  // against 34 ms with four columns per lane); deeper trees cut their long
+  // rows into many more tiles per level and take four columns per lane
+  // throughout (6.26M-vertex graph: narrow levels 500 -> 300 ms).
+  {
+    int height = 0;
+    for (const Graph *g : gs) height = std::max(height, g->tree_height);
+    scalar_cols = height <= 2048 ? 32 : 0;
+    if (const char *e = std::getenv("GPUH2H_FILL_SCALAR_COLS")) scalar_cols = std::max(0, std::atoi(e));
+  }
   f_seg_off[N] = seg_total;
   mark("host assembly");
   threads = 128;
@@ -724,6 +847,9 @@ FillPlan::FillPlan(const std::vector<Graph *> &graphs, const TilePolicy &pol, co
     GH_CUDA(cudaMemcpy(father, f_father.data(), sizeof(int) * N, cudaMemcpyHostToDevice));
     GH_CUDA(cudaMemcpy(depth, f_depth.data(), sizeof(int) * N, cudaMemcpyHostToDevice));
     GH_CUDA(cudaMemcpy(hld, f_hld.data(), sizeof(int) * N, cudaMemcpyHostToDevice));
+    hld_row = dalloc<int64_t>(N, work_bytes);
+    hld_row_kernel<<<std::max(1, std::min(8192, (N + 255) / 256)), 256>>>(hld, drow, hld_row, N);
+    GH_CUDA(cudaGetLastError());
     mark("allocations and uploads");
     {
       const size_t ksmem = (size_t)(max_m + 1) * sizeof(int);
@@ -756,10 +882,11 @@ FillPlan::FillPlan(const std::vector<Graph *> &graphs, const TilePolicy &pol, co
 FillPlan::~FillPlan() { release_work(); }
 
 void FillPlan::release_work() {
-  void *ps[] = {pos_w, pos_src, hld, htop, hpos, seg_off, seg_top, seg_pos, done, next, err, tiles, trace_t};
+  void *ps[] = {pos_w, pos_src, hld, htop, hpos, seg_off, seg_top, seg_pos, done, next, err, tiles, trace_t, hld_row};
   for (void *p : ps) cudaFree(p);
   trace_t = nullptr;
   pos_w = pos_src = hld = htop = hpos = seg_top = seg_pos = done = next = err = tiles = nullptr;
+  hld_row = nullptr;
   seg_off = nullptr;
 }
 
@@ -852,7 +979,7 @@ void FillPlan::build_tiles(const TilePolicy &pol) {
       sc = std::max(m, 1);
       return true;  // one tile
     }
-    cb = pol.col_block[wb][sb];
+    cb = (pol.col_block[wb][sb] + 3) & ~3;  // the sweep takes columns four at a time
     sc = pol.sep_chunk[wb][sb];
     nt_node = ((d + cb - 1) / cb) * ((std::max(m, 1) + sc - 1) / sc);
     return false;
@@ -1030,7 +1157,7 @@ void FillPlan::enqueue(cudaStream_t s, cudaEvent_t *fill_ev) {
   A.pos_id = pos_id;
   A.pos_pos = pos_pos;
   A.pos_w = pos_w;
-  A.hld = hld;
+  A.hld_row = hld_row;
   A.seg_off = seg_off;
   A.seg_top = seg_top;
   A.seg_pos = seg_pos;
@@ -1040,6 +1167,7 @@ void FillPlan::enqueue(cudaStream_t s, cudaEvent_t *fill_ev) {
   A.spin_limit = spin_limit_cycles();
   A.max_u = max_u;
   A.max_segs = std::max(max_segs, 1);
+  A.scalar_cols = scalar_cols;
   A.trace_t = nullptr;
   cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
   GH_CUDA(cudaStreamIsCapturing(s, &cs));

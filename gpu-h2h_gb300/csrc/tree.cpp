@@ -110,7 +110,7 @@ void allocate_labels_and_bfs(Graph &g) {
   Clock clk;
   const int n = g.n;
   Pool pool(g.threads);
-  prefix_sums(pool, n, g.dis_hash, [&](int64_t v) { return (int64_t)g.depth[v]; });
+  if (!g.tree_layout) prefix_sums(pool, n, g.dis_hash, [&](int64_t v) { return (int64_t)g.depth[v]; });
   prefix_sums(pool, n, g.pos_hash, [&](int64_t v) { return (int64_t)(g.x_off[v + 1] - g.x_off[v]) + 1; });
   // host position lists only for the level-synchronous fill; the dataflow
   // fill builds them on the GPU from the device lists
@@ -149,6 +149,10 @@ void allocate_labels_and_bfs(Graph &g) {
   }
   g.t.malloc_labels = clk.us();
   clk.reset();
+  if (g.tree_layout) {  // built with the tree on the GPU (tree_gpu.cu)
+    g.t.bfs = clk.us();
+    return;
+  }
   // level order from the head, children in Childs order
   g.tree_bfs.clear();
   g.tree_bfs.reserve(n);

@@ -23,7 +23,7 @@ LIB = os.path.join(OUT, "libgpuh2h.so")
 CLI = os.path.join(OUT, "G2H")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-LIB_SOURCES = ["io.cpp", "gen.cpp", "elim_sets.cu", "tree.cpp", "capi.cpp", "contract.cu", "labels.cu", "query.cu", "noalloc.cu", "batch.cpp", "server.cpp", "loadgen.cpp", "index_io.cpp"]
+LIB_SOURCES = ["io.cpp", "gen.cpp", "elim_sets.cu", "tree.cpp", "tree_gpu.cu", "capi.cpp", "contract.cu", "labels.cu", "query.cu", "noalloc.cu", "batch.cpp", "server.cpp", "loadgen.cpp", "index_io.cpp"]
 
 
 def cuda_home() -> str:
