@@ -604,7 +604,7 @@ __global__ void __launch_bounds__(512, 1) cell_grid_kernel(GridArgs H) {
   __shared__ int s_rs[32], s_rd[32], s_ri[32], s_rp[32];
   __shared__ int s_bc[4];  // v, height of the pick, |own list|, stop
   __shared__ int4 s_best;  // this block's argmin (a one-block cell reads it here)
-  __shared__ int s_nmine, s_nslot, s_flag;
+  __shared__ int s_nmine, s_nslot, s_flag, s_ntake;
   const ElimArgs &A = H.E;
   const int tid = threadIdx.x, nthr = blockDim.x, lane = tid & 31, wid = tid >> 5, nw = nthr >> 5;
   const int b = blockIdx.x;
@@ -687,6 +687,7 @@ __global__ void __launch_bounds__(512, 1) cell_grid_kernel(GridArgs H) {
       }
       if (tid == 0) {
         s_nmine = 0;
+        s_ntake = 0;
         s_bc[3] = bp < 0;  // j < k candidates remain, so a pick exists
         if (bp >= 0) {
           s_bc[0] = bi;
@@ -754,7 +755,13 @@ __global__ void __launch_bounds__(512, 1) cell_grid_kernel(GridArgs H) {
       if (owner_of(aid[i], nb) == r) mine[atomicAdd(&s_nmine, 1)] = i;
     __syncthreads();
     const int nm = s_nmine;
-    for (int t = wid; t < nm; t += nw) {
+    // warps take the block's neighbours one at a time as they finish, so a
+    // few long lists do not hold the block (and the cell's barrier) back
+    for (;;) {
+      int t = 0;
+      if (lane == 0) t = atomicAdd(&s_ntake, 1);
+      t = __shfl_sync(0xffffffffu, t, 0);
+      if (t >= nm) break;
       const int i = mine[t];
       const int u = aid[i];
       const NbrMeta m = load_meta(A, u);
