@@ -233,24 +233,30 @@ __device__ void merge_neighbour(const ElimArgs &A, int u, const NbrMeta &m, int 
   const int seg = (total_len + 31) >> 5;
   const int k0 = min(lane * seg, total_len), k1 = min(k0 + seg, total_len);
   const int i0 = corank(pid, np, aid, iu, nq, k0);
-  // pass 1: count outputs, apply matched updates to the first entry of the id
+  // pass 1: count outputs, apply matched updates to the first entry of the
+  // id.  The walk keeps the next P and Q ids, the last P id taken and the
+  // first index of its run in registers, so a step waits on one shared-memory
+  // load at most (the loads of a step no longer depend on each other).
   int cnt = 0;
   {
     int i = i0, j = k0 - i0;
+    int a = i < np ? pid[i] : 0;
+    int b = j < nq ? q_at(aid, iu, j) : 0;
+    int prev = i > 0 ? pid[i - 1] : 0, run = i - 1;  // the last P id taken and its run's first index
+    if (i > 0)
+      while (run > 0 && pid[run - 1] == prev) run--;
     for (int t = k0; t < k1; t++) {
-      if (i < np && (j >= nq || pid[i] <= q_at(aid, iu, j))) {
+      if (i < np && (j >= nq || a <= b)) {
+        if (i == 0 || a != prev) run = i;
+        prev = a;
         i++;
         cnt++;
+        a = i < np ? pid[i] : 0;
       } else {
-        const int x = q_at(aid, iu, j);
-        if (i > 0 && pid[i - 1] == x) {
-          int f = i - 1;
-          while (f > 0 && pid[f - 1] == x) f--;
-          atomicMin(pw + f, wu + q_at(aw, iu, j));
-        } else {
-          cnt++;
-        }
+        if (i > 0 && prev == b) atomicMin(pw + run, wu + q_at(aw, iu, j));
+        else cnt++;
         j++;
+        b = j < nq ? q_at(aid, iu, j) : 0;
       }
     }
   }
@@ -293,20 +299,25 @@ __device__ void merge_neighbour(const ElimArgs &A, int u, const NbrMeta &m, int 
   } else if (fits) {
     int o = incl - cnt;
     int i = i0, j = k0 - i0;
+    int a = i < np ? pid[i] : 0;
+    int b = j < nq ? q_at(aid, iu, j) : 0;
+    int prev = i > 0 ? pid[i - 1] : 0;
     for (int t = k0; t < k1; t++) {
-      if (i < np && (j >= nq || pid[i] <= q_at(aid, iu, j))) {
-        A.slot_nbr[off + Jn + o] = pid[i];
+      if (i < np && (j >= nq || a <= b)) {
+        A.slot_nbr[off + Jn + o] = a;
         A.slot_w[off + Jn + o] = pw[i];
         o++;
+        prev = a;
         i++;
+        a = i < np ? pid[i] : 0;
       } else {
-        const int x = q_at(aid, iu, j);
-        if (!(i > 0 && pid[i - 1] == x)) {
-          A.slot_nbr[off + Jn + o] = x;
+        if (!(i > 0 && prev == b)) {
+          A.slot_nbr[off + Jn + o] = b;
           A.slot_w[off + Jn + o] = wu + q_at(aw, iu, j);
           o++;
         }
         j++;
+        b = j < nq ? q_at(aid, iu, j) : 0;
       }
     }
     for (int k = lane; k < Jn; k += 32) A.slot_nbr[off + k] = INT_MAX;
@@ -536,6 +547,8 @@ struct GridArgs {
   int4 *partial;           // (deg + height, deg, id, slot) per block
   unsigned *bar;           // per cell: arrival counter
   long long spin_limit;    // bound on one barrier wait, in SM clock cycles
+  int sslots;              // merge buffers in shared memory per block (all warps' when E.pstage is unset)
+  int slot_cap;            // pooled buffers (E.pstage set): entries per buffer, a multiple of 4
 };
 
 __device__ __forceinline__ void better(int &bs, int &bd, int &bi, int &bp, int s, int d, int i, int p) {
@@ -623,14 +636,23 @@ __global__ void __launch_bounds__(512, 1) cell_grid_kernel(GridArgs H) {
   int *cdeg = cid + sal;
   int *ch = cdeg + sal;
   int *dead = ch + sal;
-  int *pid, *pw;           // this warp's merge buffers: shared memory when they fit, else global
+  // this warp's merge buffers: its own pair in shared memory when every
+  // warp's fit; otherwise a pool of sslots shared-memory pairs that a warp
+  // takes for one merge when one is free, and its own slab in global memory
+  // when none is (a merge's walk then reads global memory)
+  int *pid, *pw;
+  int *const sbuf = dead + sal;
+  int *const gpid = A.pstage ? A.pstage + ((int64_t)b * nw + wid) * 2 * (int64_t)A.lmax : nullptr;
+  const bool pooled = A.pstage != nullptr && H.sslots > 0;
   if (A.pstage) {
-    pid = A.pstage + ((int64_t)b * nw + wid) * 2 * (int64_t)A.lmax;
+    pid = gpid;
     pw = pid + A.lmax;
   } else {
-    pid = dead + sal + (int64_t)wid * 2 * lal;
+    pid = sbuf + (int64_t)wid * 2 * lal;
     pw = pid + lal;
   }
+  __shared__ unsigned s_free;  // pooled: free shared-memory buffer pairs
+  if (tid == 0) s_free = pooled ? (H.sslots >= 32 ? 0xffffffffu : (1u << H.sslots) - 1u) : 0u;
   Cand cand;
   cand.id = cid;
   cand.deg = cdeg;
@@ -769,7 +791,32 @@ __global__ void __launch_bounds__(512, 1) cell_grid_kernel(GridArgs H) {
         if (lane == 0) set_err(A.err, kErrStaging);
         continue;
       }
+      int slot = -1;
+      if (pooled) {
+        if (lane == 0 && m.s - m.J <= H.slot_cap) {
+          unsigned fm = *(volatile unsigned *)&s_free;
+          while (fm) {
+            const unsigned bit = 1u << (__ffs(fm) - 1);
+            const unsigned old = atomicAnd(&s_free, ~bit);
+            if (old & bit) { slot = __ffs(bit) - 1; break; }
+            fm = old & ~bit;
+          }
+          __threadfence_block();
+        }
+        slot = __shfl_sync(0xffffffffu, slot, 0);
+        if (slot >= 0) {
+          pid = sbuf + (int64_t)slot * 2 * H.slot_cap;
+          pw = pid + H.slot_cap;
+        } else {
+          pid = gpid;
+          pw = pid + A.lmax;
+        }
+      }
       merge_neighbour<true>(A, u, m, aw[i], i, v, hnow, aid, aw, c, pid, pw, lane, cand, ns);
+      if (slot >= 0 && lane == 0) {  // merge_neighbour ends with __syncwarp: the pair is no longer read
+        __threadfence_block();
+        atomicOr(&s_free, 1u << slot);
+      }
     }
     __syncthreads();
     // ---- after the first pick of a partition cell every key becomes live
@@ -962,6 +1009,10 @@ ElimPlan::ElimPlan(const std::vector<Graph *> &graphs) : gs(graphs) {
   // 212 + 480 to 194 + 403 ms; at 8 warps and above shared memory wins.
   int grid_smem_warps = 8;
   if (const char *e = std::getenv("GPUH2H_GRID_SMEM_WARPS")) grid_smem_warps = std::max(1, std::atoi(e));
+  // with global staging: at most this many shared-memory buffer pairs per
+  // block (GPUH2H_GRID_POOL; 0 = every merge stages in global memory)
+  int grid_pool_max = 16;
+  if (const char *e = std::getenv("GPUH2H_GRID_POOL")) grid_pool_max = std::max(0, std::min(16, std::atoi(e)));
   // cell list bounds come with the elimination sets (build_elimination_sets)
   std::vector<GraphLevels> L(K);
   int threads = 1;
@@ -1126,6 +1177,7 @@ ElimPlan::ElimPlan(const std::vector<Graph *> &graphs) : gs(graphs) {
       if (arrivals >= INT32_MAX) return false;  // the barrier counter compares as int
     }
     const int64_t own = 3 * al(4LL * lmax) + 4 * al(4LL * slice_max), per_warp = 2 * al(4LL * lmax);
+    const int lal_ints = (lmax + 3) & ~3;
     if (own > smem_dyn_g) return false;
     // per-warp merge buffers in shared memory when grid_smem_warps+ warps'
     // worth fit (a merge walks them serially), else 16 warps with buffers in
@@ -1133,7 +1185,23 @@ ElimPlan::ElimPlan(const std::vector<Graph *> &graphs) : gs(graphs) {
     const int64_t fit = (smem_dyn_g - own) / per_warp;
     const int hw = fit >= grid_smem_warps ? (int)std::min<int64_t>(16, fit) : 16;
     const bool gstage = fit < grid_smem_warps;
-    const int64_t hsmem = gstage ? own : own + hw * per_warp;
+    // with global staging, the shared memory left over holds a pool of
+    // buffer pairs that merges take while one is free (near the top of the
+    // order a block runs a handful of merges per elimination): buffers of up
+    // to slot_cap entries, at least 8 of them when room allows (the lists
+    // merged there are mostly far shorter than the longest)
+    int sslots = hw, slot_cap = lal_ints;
+    if (gstage && heap) {
+      // a global order keeps the shared memory for the L1 cache: its merges
+      // read staged lists back through it (3.6M-vertex graph: 229 ms with
+      // the pool, 217 ms without)
+      sslots = 0;
+    } else if (gstage) {
+      const int64_t avail = smem_dyn_g - own;
+      slot_cap = (int)std::min<int64_t>(lal_ints, std::max<int64_t>(512, (avail / (8 * 8)) & ~int64_t(3)));
+      sslots = (int)std::min<int64_t>(std::min<int64_t>(16, avail / (8 * (int64_t)slot_cap)), grid_pool_max);
+    }
+    const int64_t hsmem = gstage ? own + (int64_t)sslots * 8 * slot_cap : own + (int64_t)hw * per_warp;
     int per = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, cell_grid_kernel, hw * 32, (size_t)hsmem) !=
             cudaSuccess ||
@@ -1154,6 +1222,8 @@ ElimPlan::ElimPlan(const std::vector<Graph *> &graphs) : gs(graphs) {
     Lc.slots = used;
     Lc.smem = hsmem;
     Lc.global_stage = gstage;
+    Lc.sslots = sslots;
+    Lc.slot_cap = slot_cap;
     Lc.pstage_off = 0;
     Lc.grid = true;
     Lc.slice_max = slice_max;
@@ -1394,6 +1464,8 @@ void ElimPlan::launch_one(const Launch &Lc, cudaStream_t s, bool trace) {
     H.partial = (int4 *)hg_partial;
     H.bar = grid_bar + Lc.bar_off;
     H.spin_limit = spin_limit_cycles();
+    H.sslots = Lc.sslots;
+    H.slot_cap = Lc.slot_cap;
     cudaLaunchAttribute ca[1];
     ca[0].id = cudaLaunchAttributeCooperative;
     ca[0].val.cooperative = 1;
@@ -1413,10 +1485,13 @@ void ElimPlan::launch_one(const Launch &Lc, cudaStream_t s, bool trace) {
     cudaEventSynchronize(ev1);
     float ms = 0;
     cudaEventElapsedTime(&ms, ev0, ev1);
+    char pool[64] = "";
+    if (Lc.grid && Lc.global_stage) std::snprintf(pool, sizeof pool, " (pool %d x %d entries)", Lc.sslots, Lc.slot_cap);
     std::fprintf(stderr,
-                 "[gpuh2h] elim %s %d: %d cells x %d CTAs x %d warps, kmax %d, lmax %d, smem %lld, slots %d%s%s: %.3f ms\n",
+                 "[gpuh2h] elim %s %d: %d cells x %d CTAs x %d warps, kmax %d, lmax %d, smem %lld, slots %d%s%s%s: %.3f ms\n",
                  Lc.heap ? "heap" : "level", Lc.level, Lc.ncell, Lc.cs, Lc.nw, Lc.kmax, Lc.lmax, (long long)Lc.smem,
-                 Lc.slots, Lc.global_stage ? " (global merge staging)" : "", Lc.grid ? " (cooperative, slots = blocks)" : "", ms);
+                 Lc.slots, Lc.global_stage ? " (global merge staging)" : "", pool,
+                 Lc.grid ? " (cooperative, slots = blocks)" : "", ms);
     cudaEventDestroy(ev0);
     cudaEventDestroy(ev1);
   }
