@@ -301,7 +301,12 @@ int h2h_get_info(const h2h_graph *h, h2h_info *info) {
   info->t_bfs_us = t.bfs;
   info->t_translate_labels_us = t.translate_labels;
   info->t_fill_gpu_us = t.fill_gpu;
-  info->max_label = g.max_label;
+  try {
+    info->max_label = g.labelled ? gh::label_max(g) : 0;
+  } catch (const gh::Error &e) {
+    gh::set_last_error(e.what());
+    return e.code;
+  }
   info->label_updates = 0;
   if (!g.pos_hash.empty() && (int)g.depth.size() == g.n)
     for (int v = 0; v < g.n; v++)

@@ -115,7 +115,7 @@ struct Graph {
   int max_segs = 0;
   bool tree_layout = false;  // depth, first, level order, heavy paths, segments and dis_hash built on the GPU
   bool labelled = false;
-  int64_t max_label = 0;
+  int64_t max_label = 0;  // -1: not computed yet (label_max computes it)
   // device
   DeviceIndex dev;
   Timings t;
@@ -280,6 +280,7 @@ inline bool uses_level_fill(const Graph &g) {
   return g.label_mode == H2H_LABEL_L3 || std::getenv("GPUH2H_LEVEL_FILL") != nullptr;
 }
 void download_labels(const Graph &g, int *dis_out);    // labels.cu, reference layout
+int64_t label_max(const Graph &g);                     // labels.cu: largest finite label, computed once
 // labels.cu: the reference's level-by-level GPU fill mapping on a built L4
 // graph (measurement baseline): device ms and mismatches against the labels
 void fill_labels_plain(const Graph &g, int mapping, double *ms, int64_t *mismatches);

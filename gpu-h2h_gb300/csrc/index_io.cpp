@@ -129,7 +129,7 @@ int h2h_save_index(const h2h_graph *h, const char *path) {
     hd.x_total = g.x_off[n];
     hd.pos_total = np;
     hd.label_total = g.dis_hash[n];
-    hd.max_label = g.max_label;
+    hd.max_label = gh::label_max(g);
     hd.decomposition_size = g.decomposition_size;
     hd.H = g.H_cli;
     hd.C = g.C;

@@ -12,7 +12,8 @@
 // is a closed form over subtree sizes and sums along root paths:
 //   * children: a stable radix sort of (father, v) pairs, v ascending;
 //   * subtree sizes: bottom-up, one thread per leaf climbing while it is the
-//     last child of its father to arrive (an arrival counter per node);
+//     last child of its father to arrive (one 64-bit word per node holds the
+//     children still to come and the sizes already brought);
 //   * a child c of p is entered in the tour at first(p) + 1 + 2 * (sizes of
 //     the siblings before c), and p follows c's subtree at first(c) +
 //     2 * size(c) - 1; the preorder index is (first + depth - 1) / 2;
@@ -231,30 +232,38 @@ __global__ void child_key_kernel(const int *father, int n, unsigned *key, int *v
   }
 }
 
-// Subtree sizes: a thread starts at every leaf and climbs; at each father it
-// adds its subtree's size and counts itself in; the child that completes the
-// count carries on with the father's finished size.  Every node is climbed
-// past once, so the walk is O(n); a thread stops after n steps whatever the
-// input.
-__global__ void subtree_size_kernel(const int *father, const int *cnt, int *pending, int *acc, int *size, int n,
+// Subtree sizes: a thread starts at every leaf and climbs.  Each node has
+// one 64-bit word: children still to arrive in the high half, the sizes
+// they brought in the low half.  A child adds its size and takes one off
+// the count in a single atomic; the child that sees the count reach zero
+// knows the father's size from the value it got back and carries on.  One
+// atomic per step (a chain as long as the tree is tall); every node is
+// climbed past once, so the walk is O(n); a thread stops after n steps
+// whatever the input.
+__global__ void subtree_size_kernel(const int *father, const int *cnt, unsigned long long *word, int *size, int n,
                                     int *err) {
   for (int v0 = blockIdx.x * blockDim.x + threadIdx.x; v0 < n; v0 += gridDim.x * blockDim.x) {
     if (cnt[v0] != 0) continue;
-    int v = v0, sz = 1;
+    int v = v0;
+    unsigned long long sz = 1;
     size[v] = 1;
     for (int step = 0; step < n; step++) {
       const int p = father[v];
       if (p < 0) break;
       if (p >= n) { flag_err(err); break; }
-      atomicAdd(acc + p, sz);
-      __threadfence();
-      if (atomicSub(pending + p, 1) != 1) break;  // a sibling is still climbing
-      __threadfence();
-      sz = atomicAdd(acc + p, 0) + 1;
-      size[p] = sz;
+      const unsigned long long old = atomicAdd(word + p, sz - (1ull << 32));
+      if ((old >> 32) != 1) break;  // a sibling is still climbing
+      sz = (old & 0xffffffffull) + sz + 1;
+      size[p] = (int)sz;
       v = p;
     }
   }
+}
+
+// Arrival words: the child count of every node in the high half.
+__global__ void arrival_word_kernel(const int *cnt, unsigned long long *word, int n) {
+  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x)
+    word[v] = (unsigned long long)cnt[v] << 32;
 }
 
 // Per father, over its children in id order: the heavy child (largest
@@ -422,11 +431,12 @@ void build_tree_gpu(Graph &g) {
   }
   const int *childs = val;  // the first n - 1 sorted values (the root's key sorts last)
   // subtree sizes
-  int *pending = ws.get<int>(n), *acc = ws.get<int>(n), *size = ws.get<int>(n);
-  GH_CUDA(cudaMemcpy(pending, cnt, sizeof(int) * n, cudaMemcpyDeviceToDevice));
-  GH_CUDA(cudaMemset(acc, 0, sizeof(int) * n));
+  unsigned long long *word = ws.get<unsigned long long>(n);
+  int *size = ws.get<int>(n);
+  arrival_word_kernel<<<grid, 256, 0, s>>>(cnt, word, n);
+  GH_CUDA(cudaGetLastError());
   GH_CUDA(cudaMemset(size, 0, sizeof(int) * n));
-  subtree_size_kernel<<<grid, 256, 0, s>>>(father, cnt, pending, acc, size, n, err);
+  subtree_size_kernel<<<grid, 256, 0, s>>>(father, cnt, word, size, n, err);
   GH_CUDA(cudaGetLastError());
   {
     int sz_root = 0;

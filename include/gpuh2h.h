@@ -115,7 +115,9 @@ typedef struct {
   double lub_mb, decomposition_tree_mb, rmq_mb, label_mb;
   int64_t t_load_us, t_rank_tree_us, t_lub_us, t_translate_lub_us, t_td_gpu_us, t_translate_back_us,
       t_td_cpu_us, t_tree_us, t_malloc_us, t_bfs_us, t_translate_labels_us, t_fill_gpu_us;
-  int64_t max_label;                  /* largest finite label value               */
+  int64_t max_label;                  /* largest finite label value (computed on the
+                                         first request after a build: one pass over
+                                         the labels)                               */
   int64_t label_updates;              /* sum over v of m(v)*(d(v)-2): min-plus updates of the L4 fill */
 } h2h_info;
 int h2h_get_info(const h2h_graph *g, h2h_info *info);
