@@ -2,6 +2,7 @@
 // include/gpuh2h_tools.h.  Every call converts internal exceptions into a
 // status code and a per-thread message; nothing exits the process.
 #include <algorithm>
+#include <atomic>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -9,6 +10,7 @@
 #include "gen.h"
 #include "gpuh2h_tools.h"
 #include "handle.h"
+#include "pool.h"
 
 namespace gh {
 void write_partition_rate(const Graph &g, const std::string &dir);
@@ -29,34 +31,63 @@ using gh::guarded;
 
 // Every arc u->v needs a reverse arc v->u: the partition-level kernel applies
 // the reference's pairwise fill-in per neighbour, which is the same only when
-// "u lists v" is symmetric (true for the both-directions Edge format).
-void check_symmetric(const gh::Graph &g) {
-  std::vector<uint64_t> a, b;
-  a.reserve(g.m);
-  for (int v = 0; v < g.n; v++)
-    for (int e = g.adj_off[v]; e < g.adj_off[v + 1]; e++) a.push_back(((uint64_t)v << 32) | (uint32_t)g.adj_v[e]);
-  std::sort(a.begin(), a.end());
-  a.erase(std::unique(a.begin(), a.end()), a.end());
-  b.resize(a.size());
-  for (size_t i = 0; i < a.size(); i++) b[i] = (a[i] << 32) | (a[i] >> 32);
-  std::sort(b.begin(), b.end());
-  GH_CHECK(a == b, H2H_ERR_UNSUPPORTED, "Edge file lists an arc without its reverse arc");
+// "u lists v" is symmetric (true for the both-directions Edge format).  Per
+// vertex in parallel: each vertex's neighbours sorted once, then every arc
+// u->v looks u up among v's neighbours (parallel arcs count once, as sets).
+void check_symmetric(const gh::Graph &g, gh::Pool &pool) {
+  std::vector<int> sorted(g.adj_v.begin(), g.adj_v.end());
+  pool.parallel_for(g.n, 4096, [&](int64_t lo, int64_t hi, int) {
+    for (int64_t v = lo; v < hi; v++) std::sort(sorted.begin() + g.adj_off[v], sorted.begin() + g.adj_off[v + 1]);
+  });
+  std::atomic<bool> bad{false};
+  pool.parallel_for(g.n, 4096, [&](int64_t lo, int64_t hi, int) {
+    for (int64_t u = lo; u < hi && !bad.load(std::memory_order_relaxed); u++)
+      for (int e = g.adj_off[u]; e < g.adj_off[u + 1]; e++) {
+        const int v = g.adj_v[e];
+        if (!std::binary_search(sorted.begin() + g.adj_off[v], sorted.begin() + g.adj_off[v + 1], (int)u)) {
+          bad = true;
+          break;
+        }
+      }
+  });
+  GH_CHECK(!bad.load(), H2H_ERR_UNSUPPORTED, "Edge file lists an arc without its reverse arc");
 }
 
-void check_connected(const gh::Graph &g) {
-  std::vector<char> seen(g.n, 0);
-  std::vector<int> st{0};
-  seen[0] = 1;
-  int cnt = 1;
-  while (!st.empty()) {
-    int v = st.back();
-    st.pop_back();
-    for (int e = g.adj_off[v]; e < g.adj_off[v + 1]; e++) {
-      int u = g.adj_v[e];
-      if (!seen[u]) { seen[u] = 1; cnt++; st.push_back(u); }
+// Connectivity by union-find over the arcs in parallel (lock-free: a root
+// is linked under the other by compare-and-swap, the larger id under the
+// smaller; finds halve their paths).
+void check_connected(const gh::Graph &g, gh::Pool &pool) {
+  std::vector<std::atomic<int>> parent(g.n);
+  for (int v = 0; v < g.n; v++) parent[v].store(v, std::memory_order_relaxed);
+  auto find = [&](int x) {
+    for (;;) {
+      int p = parent[x].load(std::memory_order_relaxed);
+      if (p == x) return x;
+      const int gp = parent[p].load(std::memory_order_relaxed);
+      if (gp != p) parent[x].compare_exchange_weak(p, gp, std::memory_order_relaxed);
+      x = gp;
     }
-  }
-  GH_CHECK(cnt == g.n, H2H_ERR_UNSUPPORTED,
+  };
+  pool.parallel_for(g.n, 4096, [&](int64_t lo, int64_t hi, int) {
+    for (int64_t u = lo; u < hi; u++)
+      for (int e = g.adj_off[u]; e < g.adj_off[u + 1]; e++) {
+        int a = find((int)u), b = find(g.adj_v[e]);
+        while (a != b) {
+          if (a > b) std::swap(a, b);
+          int expect = b;  // link root b under a
+          if (parent[b].compare_exchange_strong(expect, a, std::memory_order_relaxed)) break;
+          a = find(a);
+          b = find(b);
+        }
+      }
+  });
+  std::atomic<bool> split{false};
+  const int r0 = find(0);
+  pool.parallel_for(g.n, 4096, [&](int64_t lo, int64_t hi, int) {
+    for (int64_t v = lo; v < hi; v++)
+      if (find((int)v) != r0) { split = true; break; }
+  });
+  GH_CHECK(!split.load(), H2H_ERR_UNSUPPORTED,
            "graph is disconnected (the reference's elimination reads out of bounds on such input)");
 }
 
@@ -79,8 +110,13 @@ int load_common(const std::string &edge, const std::string &idf, const std::stri
     g.method = method;
     gh::load_graph(g, edge, idf, cut);
     GH_CHECK(g.C <= g.H, H2H_ERR_ARG, "ChangeToGlobalHeight exceeds the partition height");
-    check_symmetric(g);
-    check_connected(g);
+    gh::Clock clk;
+    {
+      gh::Pool pool(g.threads);
+      check_symmetric(g, pool);
+      check_connected(g, pool);
+    }
+    g.t.load += clk.us();  // the load phase includes the input checks
   });
   if (rc != H2H_OK) { delete h; return rc; }
   *out = h;

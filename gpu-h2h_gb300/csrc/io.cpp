@@ -2,9 +2,13 @@
 // (Graph_Fundamental.cu:4-95), the CSV writers (GraphPartition.cu:252-265,
 // TreeStructure.cu:54-99, Graph_Fundamental.cu:132-170, Query.cu:597-622).
 // The synthetic road-graph generator that writes those formats is gen.cpp.
+#include <fcntl.h>
 #include <sys/stat.h>
+#include <unistd.h>
 
 #include <algorithm>
+#include <atomic>
+#include <memory>
 #include <cmath>
 #include <cstring>
 #include <fstream>
@@ -18,20 +22,48 @@ namespace gh {
 
 namespace {
 
-std::string read_file(const std::string &path) {
-  FILE *f = std::fopen(path.c_str(), "rb");
-  if (!f) throw Error(H2H_ERR_IO, "cannot open " + path);
-  std::string s;
-  std::fseek(f, 0, SEEK_END);
-  long sz = std::ftell(f);
-  std::fseek(f, 0, SEEK_SET);
-  s.resize(sz > 0 ? (size_t)sz : 0);
-  if (sz > 0 && std::fread(&s[0], 1, (size_t)sz, f) != (size_t)sz) {
-    std::fclose(f);
-    throw Error(H2H_ERR_IO, "short read on " + path);
+// A whole file in memory, read by several threads at once (pread of 16 MB
+// pieces into an uninitialised buffer).
+struct FileBytes {
+  std::unique_ptr<char[]> data;
+  size_t size = 0;
+};
+
+FileBytes read_file(const std::string &path, int threads) {
+  const int fd = ::open(path.c_str(), O_RDONLY);
+  if (fd < 0) throw Error(H2H_ERR_IO, "cannot open " + path);
+  struct stat st;
+  if (::fstat(fd, &st) != 0) {
+    ::close(fd);
+    throw Error(H2H_ERR_IO, "cannot stat " + path);
   }
-  std::fclose(f);
-  return s;
+  FileBytes f;
+  f.size = st.st_size > 0 ? (size_t)st.st_size : 0;
+  f.data.reset(new char[f.size + 1]);
+  const size_t piece = size_t(16) << 20;
+  const int64_t np = (int64_t)((f.size + piece - 1) / piece);
+  std::atomic<bool> ok{true};
+  auto read_pieces = [&](int64_t lo, int64_t hi, int) {
+    for (int64_t k = lo; k < hi; k++) {
+      size_t at = (size_t)k * piece;
+      const size_t end = std::min(f.size, at + piece);
+      while (at < end) {
+        const ssize_t r = ::pread(fd, f.data.get() + at, end - at, (off_t)at);
+        if (r <= 0) { ok = false; break; }
+        at += (size_t)r;
+      }
+    }
+  };
+  if (np > 1 && threads > 1) {
+    Pool pool(std::min<int64_t>(threads, np));
+    pool.parallel_for(np, 1, read_pieces);
+  } else {
+    read_pieces(0, np, 0);
+  }
+  ::close(fd);
+  if (!ok.load()) throw Error(H2H_ERR_IO, "short read on " + path);
+  f.data[f.size] = 0;
+  return f;
 }
 
 // Whitespace tokenizer with the istream >> semantics the reference relies on.
@@ -39,6 +71,7 @@ struct Cursor {
   const char *p, *e;
   std::string what;
   explicit Cursor(const std::string &s, std::string w) : p(s.data()), e(s.data() + s.size()), what(std::move(w)) {}
+  explicit Cursor(const FileBytes &f, std::string w) : p(f.data.get()), e(f.data.get() + f.size), what(std::move(w)) {}
   void skip() {
     while (p < e && (*p == ' ' || *p == '\n' || *p == '\r' || *p == '\t' || *p == '\v' || *p == '\f')) p++;
   }
@@ -243,7 +276,7 @@ bool parse_ids_parallel(const Cursor &c0, int n, int threads, std::vector<int> &
 void load_graph(Graph &g, const std::string &edge, const std::string &idf, const std::string &cutf) {
   Clock clk;
   {
-    std::string s = read_file(idf);
+    const FileBytes s = read_file(idf, g.threads);
     Cursor c(s, idf);
     long long n = c.integer();
     GH_CHECK(n > 0 && n < INT32_MAX, H2H_ERR_FORMAT, "bad vertex count in " + idf);
@@ -267,7 +300,7 @@ void load_graph(Graph &g, const std::string &edge, const std::string &idf, const
       GH_CHECK(g.part_ids[i] >= 0 && g.id_hash[i] >= 0, H2H_ERR_FORMAT, idf + " is not a permutation");
   }
   {
-    std::string s = read_file(edge);
+    const FileBytes s = read_file(edge, g.threads);
     Cursor c(s, edge);
     long long n2 = c.integer(), m = c.integer();
     GH_CHECK(n2 == g.n, H2H_ERR_FORMAT, "vertex count of " + edge + " differs from " + idf);
@@ -286,22 +319,45 @@ void load_graph(Graph &g, const std::string &edge, const std::string &idf, const
         eu.push_back((int)a - 1); ev.push_back((int)b - 1); ew.push_back((int)w);
       }
     }
-    std::vector<int> cnt(g.n + 1, 0);
-    for (int a : eu) cnt[a]++;
     g.m = (int64_t)eu.size();
+    // adjList in file order (push_back): when the arcs already come grouped
+    // by tail in increasing order, as Edge files are written, the lists are
+    // the arc arrays themselves and the offsets the group starts (found in
+    // parallel); otherwise a counting pass and a placement pass
+    Pool pool(std::max(1, g.threads));
+    std::atomic<bool> sorted{true};
+    pool.parallel_for(g.m, 1 << 16, [&](int64_t lo, int64_t hi, int) {
+      for (int64_t i = std::max<int64_t>(lo, 1); i < hi; i++)
+        if (eu[i] < eu[i - 1]) { sorted = false; break; }
+    });
     g.adj_off.assign(g.n + 1, 0);
-    for (int i = 0; i < g.n; i++) g.adj_off[i + 1] = g.adj_off[i] + cnt[i];
-    g.adj_v.resize(g.m);
-    g.adj_w.resize(g.m);
-    std::vector<int> fill(g.adj_off.begin(), g.adj_off.end() - 1);
-    for (int64_t i = 0; i < g.m; i++) {                   // push_back keeps file order
-      int k = fill[eu[i]]++;
-      g.adj_v[k] = ev[i];
-      g.adj_w[k] = ew[i];
+    if (sorted.load()) {
+      // adj_off[u] = the first arc whose tail is >= u
+      pool.parallel_for(g.m + 1, 1 << 16, [&](int64_t lo, int64_t hi, int) {
+        for (int64_t i = lo; i < hi; i++) {
+          const int prev = i == 0 ? -1 : eu[i - 1];
+          const int cur = i == g.m ? g.n : eu[i];
+          for (int u = prev + 1; u <= cur; u++) g.adj_off[u] = (int)i;
+        }
+      });
+      g.adj_v.swap(ev);
+      g.adj_w.swap(ew);
+    } else {
+      std::vector<int> cnt(g.n + 1, 0);
+      for (int a : eu) cnt[a]++;
+      for (int i = 0; i < g.n; i++) g.adj_off[i + 1] = g.adj_off[i] + cnt[i];
+      g.adj_v.resize(g.m);
+      g.adj_w.resize(g.m);
+      std::vector<int> fill(g.adj_off.begin(), g.adj_off.end() - 1);
+      for (int64_t i = 0; i < g.m; i++) {                 // push_back keeps file order
+        int k = fill[eu[i]]++;
+        g.adj_v[k] = ev[i];
+        g.adj_w[k] = ew[i];
+      }
     }
   }
   {
-    std::string s = read_file(cutf);
+    const FileBytes s = read_file(cutf, 1);
     Cursor c(s, cutf);
     long long hf = c.integer();
     GH_CHECK(hf >= 1 && hf <= 30, H2H_ERR_FORMAT, "bad partition height in " + cutf);

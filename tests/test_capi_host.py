@@ -174,6 +174,40 @@ def test_oracle_generators_equal_library_generators(tmp_path):
     o.close()
 
 
+def test_loader_keeps_file_order_for_ungrouped_arcs(tmp_path):
+    """adjList is push_back in file order (Graph_Fundamental.cu:46-55): an Edge
+    file whose arcs are not grouped by tail loads into the same lists as a
+    plain stable grouping of its lines, with self loops dropped."""
+    import shutil
+
+    import gpuh2h
+    root = str(tmp_path)
+    gpuh2h.generate_road(root, "cfg0")
+    e, i, c = gpuh2h.files_for(root, "cfg0")
+    lines = open(e).read().split("\n")
+    n, m = map(int, lines[0].split())
+    arcs = [l for l in lines[1:] if l.strip()]
+    rng = np.random.default_rng(5)
+    arcs = [arcs[k] for k in rng.permutation(len(arcs))] + ["a 7 7 5"]  # plus a self loop
+    os.makedirs(os.path.join(root, "Partition", "shuf"), exist_ok=True)
+    with open(os.path.join(root, "Graph", "USA", "shufEdge.txt"), "w") as f:
+        f.write("%d %d\n" % (n, len(arcs)) + "\n".join(arcs) + "\n")
+    shutil.copy(i, os.path.join(root, "Partition", "shuf", "LatitudeID.txt"))
+    shutil.copy(c, os.path.join(root, "Partition", "shuf", "LatitudeCut.txt"))
+    g = gpuh2h.Graph("shuf", 6, 1, 4, 1, files=gpuh2h.files_for(root, "shuf"))
+    off, v, w = g.input_arcs()
+    lists = [[] for _ in range(n)]
+    for l in arcs:
+        _, a, b, ww = l.split()
+        if a != b:
+            lists[int(a) - 1].append((int(b) - 1, int(ww)))
+    assert off[-1] == sum(len(x) for x in lists)
+    for u in range(0, n, 37):
+        got = list(zip(v[off[u]:off[u + 1]].tolist(), w[off[u]:off[u + 1]].tolist()))
+        assert got == lists[u], u
+    g.close()
+
+
 def test_g2h_cli_argument_count_rule(tmp_path):
     from gpuh2h import _build
     _build.build()
