@@ -51,6 +51,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <exception>
+#include <memory>
 #include <queue>
 
 #include "graph.h"
@@ -1644,7 +1645,8 @@ void download_lists(Graph &g) {
 void contract_gpu(Graph &g) {
   Clock clk;
   const bool trace = std::getenv("GPUH2H_TRACE") != nullptr;
-  ElimPlan plan({&g});
+  auto owned = std::make_unique<ElimPlan>(std::vector<Graph *>{&g});
+  ElimPlan &plan = *owned;
   GH_CUDA(cudaDeviceSynchronize());
   g.t.translate_lub = clk.us();
   clk.reset();
@@ -1669,6 +1671,7 @@ void contract_gpu(Graph &g) {
   g.t.td_cpu = heap_us;             // global order over levels <= C (TDInCPUTime in the reference, on the GPU here)
   clk.reset();
   plan.build_lists();
+  owned.reset();  // the elimination's device state is freed here, inside the timed phase
   g.t.translate_back = clk.us();
 }
 

@@ -1403,7 +1403,10 @@ void fill_labels_gpu(Graph &g) {
     cudaEventDestroy(ev[0]);
     cudaEventDestroy(ev[1]);
     g.t.fill_gpu = (long long)(ms * 1000.0f);
+    Clock tail;  // the per-graph view and the plan's work buffers count with the plan's host time
     plan.attach(true);
+    plan.release_work();
+    g.t.translate_labels += tail.us();
     return;
   }
   D.release_labels();
