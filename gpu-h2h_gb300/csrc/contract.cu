@@ -99,6 +99,24 @@ struct Cand {
   int *id, *deg, *third;
 };
 
+// ints [at, at + n) of the arena, or -1 when it has no room (lane 0 asks,
+// every lane gets the answer).
+__device__ __forceinline__ int arena_take(int *next, int cap, int n, int lane) {
+  int at = -1;
+  if (lane == 0) {
+    int cur = *(volatile int *)next;
+    while (cur + n <= cap) {
+      const int old = atomicCAS(next, cur, cur + n);
+      if (old == cur) {
+        at = cur;
+        break;
+      }
+      cur = old;
+    }
+  }
+  return __shfl_sync(0xffffffffu, at, 0);
+}
+
 __device__ __forceinline__ bool key_less(int s1, int d1, int i1, int s2, int d2, int i2) {
   if (s1 != s2) return s1 < s2;
   if (d1 != d2) return d1 < d2;
@@ -117,6 +135,54 @@ __device__ __forceinline__ int corank(const int *pid, int np, const int *aid, in
     if (pid[mid] <= q_at(aid, iu, k - 1 - mid)) lo = mid + 1; else hi = mid;
   }
   return lo;
+}
+
+// The duplicate merge of a picked vertex's own list (kernel_functions.cu:
+// 338-361), by one warp.  The reference walks the list once: an entry equal
+// to its predecessor takes the smaller of the two weights and the predecessor
+// becomes INT_MAX, then the INT_MAX entries are compacted out.  So of every
+// run of equal ids only the last entry stays, carrying the run's smallest
+// weight, and entries that were INT_MAX already go too.  Here that is a
+// segmented minimum over runs, 32 entries at a time (the run minimum crosses
+// chunk boundaries in a register), and a stable compaction in place: an entry
+// lands at or before its own index, after the warp has read the chunk and the
+// entry that follows it.  Returns the new length in every lane.
+__device__ int collapse_runs_warp(int *aid, int *aw, int sv, int lane) {
+  int out = 0, last_id = INT_MAX, carry = INT_MAX;
+  for (int base = 0; base < sv; base += 32) {
+    const int i = base + lane;
+    const bool valid = i < sv;
+    const int x = valid ? aid[i] : INT_MAX;
+    int w = valid ? aw[i] : INT_MAX;
+    const int nx = i + 1 < sv ? aid[i + 1] : INT_MAX;
+    const int px = __shfl_up_sync(0xffffffffu, x, 1);
+    const int prev = lane == 0 ? last_id : px;
+    const bool real = valid && x != INT_MAX;
+    int f = !(real && x == prev && i > 0);  // head of a run
+    if (lane == 0 && !f) w = min(w, carry);
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int wy = __shfl_up_sync(0xffffffffu, w, o);
+      const int fy = __shfl_up_sync(0xffffffffu, f, o);
+      if (lane >= o) {
+        if (!f) w = min(w, wy);
+        f |= fy;
+      }
+    }
+    const bool keep = real && (i + 1 >= sv || nx != x);
+    const unsigned bal = __ballot_sync(0xffffffffu, keep);
+    last_id = __shfl_sync(0xffffffffu, x, 31);
+    carry = __shfl_sync(0xffffffffu, w, 31);
+    __syncwarp();
+    if (keep) {
+      const int o = out + __popc(bal & ((1u << lane) - 1u));
+      aid[o] = x;
+      aw[o] = w;
+    }
+    out += __popc(bal);
+    __syncwarp();
+  }
+  return out;
 }
 
 // What a merge needs to know about neighbour u, loaded in one round trip:
@@ -152,7 +218,7 @@ __device__ __forceinline__ NbrMeta load_meta(const ElimArgs &A, int u) {
 // the merge's latency.  The slot arrays are padded by four entries, so a
 // vector that starts inside the list never leaves the allocation.
 template <bool kWide>
-__device__ void merge_neighbour(const ElimArgs &A, int u, const NbrMeta &m, int wu, int iu, int v, int hnow,
+__device__ __forceinline__ void merge_neighbour(const ElimArgs &A, int u, const NbrMeta &m, int wu, int iu, int v, int hnow,
                                 const int *aid, const int *aw, int c, int *pid, int *pw, int lane, Cand cand,
                                 int nslots) {
   int64_t off = m.off;
@@ -237,7 +303,11 @@ __device__ void merge_neighbour(const ElimArgs &A, int u, const NbrMeta &m, int 
   // pass 1: count outputs, apply matched updates to the first entry of the
   // id.  The walk keeps the next P and Q ids, the last P id taken and the
   // first index of its run in registers, so a step waits on one shared-memory
-  // load at most (the loads of a step no longer depend on each other).
+  // load at most (the loads of a step no longer depend on each other).  Q's
+  // ids are distinct (v's list is sorted and its duplicates were merged), so
+  // a run of P receives at most one update, from the one lane that meets
+  // its Q entry: a plain read-min-write (a shared-memory atomic costs more),
+  // ordered before pass 2's reads by the __syncwarp between the passes.
   int cnt = 0;
   {
     int i = i0, j = k0 - i0;
@@ -254,8 +324,12 @@ __device__ void merge_neighbour(const ElimArgs &A, int u, const NbrMeta &m, int 
         cnt++;
         a = i < np ? pid[i] : 0;
       } else {
-        if (i > 0 && prev == b) atomicMin(pw + run, wu + q_at(aw, iu, j));
-        else cnt++;
+        if (i > 0 && prev == b) {
+          const int x = wu + q_at(aw, iu, j);
+          if (x < pw[run]) pw[run] = x;
+        } else {
+          cnt++;
+        }
         j++;
         b = j < nq ? q_at(aid, iu, j) : 0;
       }
@@ -291,8 +365,8 @@ __device__ void merge_neighbour(const ElimArgs &A, int u, const NbrMeta &m, int 
   }
   if (fits && total == np && Jn == 0) {
     // no insert (every member of Q is already in P, as near the top of the
-    // order): the output is P with its matched entries min-updated by pass
-    // 1, written contiguously
+    // order): the output is P with its matched entries min-updated, written
+    // contiguously
     for (int k = lane; k < np; k += 32) {
       A.slot_nbr[off + k] = pid[k];
       A.slot_w[off + k] = pw[k];
@@ -371,14 +445,14 @@ __global__ void __maxnreg__(48) elim_kernel(ElimArgs A) {
   mine.third = (int *)take(sizeof(int) * A.kmax);
   int *aid = (int *)take(sizeof(int) * A.lmax);
   int *aw = (int *)take(sizeof(int) * A.lmax);
-  int *pid, *pw;
-  if (A.pstage) {  // lists too long for shared memory: this warp's slab of the global staging
-    int *slab = A.pstage + ((int64_t)blockIdx.x * nw + wid) * 2 * (int64_t)A.lmax;
-    pid = slab;
-    pw = slab + A.lmax;
-  } else {
-    pid = (int *)take(sizeof(int) * A.lmax * nw) + (int64_t)wid * A.lmax;
-    pw = (int *)take(sizeof(int) * A.lmax * nw) + (int64_t)wid * A.lmax;
+  // this warp's merge buffers: in shared memory, or (lists too long for it)
+  // its slab of the global staging; the merge is inlined once for each, so
+  // the shared-memory copy uses shared-space loads and stores
+  int *const gslab = A.pstage ? A.pstage + ((int64_t)blockIdx.x * nw + wid) * 2 * (int64_t)A.lmax : nullptr;
+  int *spid = (int *)smem, *spw = (int *)smem;
+  if (!A.pstage) {
+    spid = (int *)take(sizeof(int) * A.lmax * nw) + (int64_t)wid * A.lmax;
+    spw = (int *)take(sizeof(int) * A.lmax * nw) + (int64_t)wid * A.lmax;
   }
   Cand lead;  // the leader's keys through distributed shared memory
   lead.id = cluster.map_shared_rank(mine.id, 0);
@@ -454,26 +528,17 @@ __global__ void __maxnreg__(48) elim_kernel(ElimArgs A) {
         for (int i = tid + 1; i < sv; i += nthr)
           if (aid[i] == aid[i - 1]) dup = true;
       dup = __syncthreads_or(dup);
+      int cn = sv;
+      if (dup && sv <= A.lmax && wid == 0) cn = collapse_runs_warp(aid, aw, sv, lane);
       if (tid == 0) {
-        int c = sv;
         if (sv > A.lmax) {
           set_err(A.err, kErrStaging);
           s_bc[3] = 1;
         } else {
-          if (dup) {  // carry merge (the later entry keeps the smaller weight), then compaction
-            for (int i = 1; i < sv; i++) {
-              if (aid[i] == aid[i - 1] && aid[i] != INT_MAX) {
-                if (aw[i - 1] < aw[i]) aw[i] = aw[i - 1];
-                aid[i - 1] = INT_MAX;
-              }
-            }
-            c = 0;
-            for (int i = 0; i < sv; i++) if (aid[i] != INT_MAX) { aid[c] = aid[i]; aw[c] = aw[i]; c++; }
-          }
-          if (c == 0 && !A.heap_mode) { set_err(A.err, kErrEmpty); s_bc[3] = 1; }
-          else { A.lsize[v] = c; A.ljunk[v] = 0; }
+          if (cn == 0 && !A.heap_mode) { set_err(A.err, kErrEmpty); s_bc[3] = 1; }
+          else { A.lsize[v] = cn; A.ljunk[v] = 0; }
         }
-        s_bc[2] = c;
+        s_bc[2] = cn;
       }
       __syncthreads();
       const int c = s_bc[2];
@@ -496,7 +561,10 @@ __global__ void __maxnreg__(48) elim_kernel(ElimArgs A) {
           if (lane == 0) set_err(A.err, kErrStaging);
           continue;
         }
-        merge_neighbour<false>(A, u, m, aw[i], i, v, hnow, aid, aw, c, pid, pw, lane, lead, k);
+        if (gslab)
+          merge_neighbour<false>(A, u, m, aw[i], i, v, hnow, aid, aw, c, gslab, gslab + A.lmax, lane, lead, k);
+        else
+          merge_neighbour<false>(A, u, m, aw[i], i, v, hnow, aid, aw, c, spid, spw, lane, lead, k);
       }
     }
     cluster.sync();  // no CTA leaves while a peer may still read the leader's shared memory
@@ -548,8 +616,7 @@ struct GridArgs {
   int4 *partial;           // (deg + height, deg, id, slot) per block
   unsigned *bar;           // per cell: arrival counter
   long long spin_limit;    // bound on one barrier wait, in SM clock cycles
-  int sslots;              // merge buffers in shared memory per block (all warps' when E.pstage is unset)
-  int slot_cap;            // pooled buffers (E.pstage set): entries per buffer, a multiple of 4
+  int arena_ints;          // E.pstage set: ints of shared memory that merges take buffers from, per pick
 };
 
 __device__ __forceinline__ void better(int &bs, int &bd, int &bi, int &bp, int s, int d, int i, int p) {
@@ -637,23 +704,20 @@ __global__ void __launch_bounds__(512, 1) cell_grid_kernel(GridArgs H) {
   int *cdeg = cid + sal;
   int *ch = cdeg + sal;
   int *dead = ch + sal;
-  // this warp's merge buffers: its own pair in shared memory when every
-  // warp's fit; otherwise a pool of sslots shared-memory pairs that a warp
-  // takes for one merge when one is free, and its own slab in global memory
-  // when none is (a merge's walk then reads global memory)
-  int *pid, *pw;
-  int *const sbuf = dead + sal;
-  int *const gpid = A.pstage ? A.pstage + ((int64_t)b * nw + wid) * 2 * (int64_t)A.lmax : nullptr;
-  const bool pooled = A.pstage != nullptr && H.sslots > 0;
-  if (A.pstage) {
-    pid = gpid;
-    pw = pid + A.lmax;
-  } else {
-    pid = sbuf + (int64_t)wid * 2 * lal;
-    pw = pid + lal;
+  // this warp's merge buffers: a pair sized to the list, cut from a
+  // shared-memory arena that is handed out afresh at every pick, or its own
+  // slab in global memory when the arena has no room left (a merge then
+  // reads global memory, one round trip per step of a walk).  The merge is
+  // inlined twice, so the shared-memory copy addresses its buffers as
+  // shared memory (shared-space loads, not generic ones).
+  if (A.pstage == nullptr) {  // the host always provides the global slabs
+    if (tid == 0 && r == 0) set_err(A.err, kErrStaging);
+    return;
   }
-  __shared__ unsigned s_free;  // pooled: free shared-memory buffer pairs
-  if (tid == 0) s_free = pooled ? (H.sslots >= 32 ? 0xffffffffu : (1u << H.sslots) - 1u) : 0u;
+  int *const sbuf = dead + sal;
+  int *const gpid = A.pstage + ((int64_t)b * nw + wid) * 2 * (int64_t)A.lmax;
+  const bool pooled = H.arena_ints > 0;
+  __shared__ int s_arena;  // pooled: arena ints taken in this pick
   Cand cand;
   cand.id = cid;
   cand.deg = cdeg;
@@ -752,32 +816,25 @@ __global__ void __launch_bounds__(512, 1) cell_grid_kernel(GridArgs H) {
     for (int i = tid + 1; i < sv; i += nthr)
       if (aid[i] == aid[i - 1]) dup = true;
     dup = __syncthreads_or(dup);
+    int cn = sv;
+    if (dup && wid == 0) cn = collapse_runs_warp(aid, aw, sv, lane);
     if (tid == 0) {
-      int c = sv;
-      if (dup) {  // carry merge (the later entry keeps the smaller weight), then compaction
-        for (int i = 1; i < sv; i++) {
-          if (aid[i] == aid[i - 1] && aid[i] != INT_MAX) {
-            if (aw[i - 1] < aw[i]) aw[i] = aw[i - 1];
-            aid[i - 1] = INT_MAX;
-          }
-        }
-        c = 0;
-        for (int i = 0; i < sv; i++) if (aid[i] != INT_MAX) { aid[c] = aid[i]; aw[c] = aw[i]; c++; }
-      }
-      if (c == 0 && !A.heap_mode) {  // a partition cell never eliminates an isolated vertex
+      if (cn == 0 && !A.heap_mode) {  // a partition cell never eliminates an isolated vertex
         if (r == 0) set_err(A.err, kErrEmpty);
         s_bc[3] = 1;
       }
-      s_bc[2] = c;
+      s_bc[2] = cn;
     }
     __syncthreads();
     if (s_bc[3]) return;
     const int c = s_bc[2];
+    if (tid == 0) s_arena = 0;  // every merge of the last pick ended before the barrier
     // ---- the neighbours this block owns
     for (int i = tid; i < c; i += nthr)
       if (owner_of(aid[i], nb) == r) mine[atomicAdd(&s_nmine, 1)] = i;
     __syncthreads();
     const int nm = s_nmine;
+    int wbase = 0, wcap = 0;  // this warp's arena pair in this pick
     // warps take the block's neighbours one at a time as they finish, so a
     // few long lists do not hold the block (and the cell's barrier) back
     for (;;) {
@@ -792,32 +849,28 @@ __global__ void __launch_bounds__(512, 1) cell_grid_kernel(GridArgs H) {
         if (lane == 0) set_err(A.err, kErrStaging);
         continue;
       }
-      int slot = -1;
+      int *sp = sbuf, scap = 0;
+      bool in_smem = false;
       if (pooled) {
-        if (lane == 0 && m.s - m.J <= H.slot_cap) {
-          unsigned fm = *(volatile unsigned *)&s_free;
-          while (fm) {
-            const unsigned bit = 1u << (__ffs(fm) - 1);
-            const unsigned old = atomicAnd(&s_free, ~bit);
-            if (old & bit) { slot = __ffs(bit) - 1; break; }
-            fm = old & ~bit;
+        const int len = m.s - m.J;
+        if (len > wcap) {  // a fresh pair from the arena (the warp's old one stays unused)
+          const int want = (len + 3) & ~3;
+          const int at = arena_take(&s_arena, H.arena_ints, 2 * want, lane);
+          if (at >= 0) {
+            wbase = at;
+            wcap = want;
           }
-          __threadfence_block();
         }
-        slot = __shfl_sync(0xffffffffu, slot, 0);
-        if (slot >= 0) {
-          pid = sbuf + (int64_t)slot * 2 * H.slot_cap;
-          pw = pid + H.slot_cap;
-        } else {
-          pid = gpid;
-          pw = pid + A.lmax;
+        if (len <= wcap) {
+          sp = sbuf + wbase;
+          scap = wcap;
+          in_smem = true;
         }
       }
-      merge_neighbour<true>(A, u, m, aw[i], i, v, hnow, aid, aw, c, pid, pw, lane, cand, ns);
-      if (slot >= 0 && lane == 0) {  // merge_neighbour ends with __syncwarp: the pair is no longer read
-        __threadfence_block();
-        atomicOr(&s_free, 1u << slot);
-      }
+      if (in_smem)
+        merge_neighbour<true>(A, u, m, aw[i], i, v, hnow, aid, aw, c, sp, sp + scap, lane, cand, ns);
+      else
+        merge_neighbour<true>(A, u, m, aw[i], i, v, hnow, aid, aw, c, gpid, gpid + A.lmax, lane, cand, ns);
     }
     __syncthreads();
     // ---- after the first pick of a partition cell every key becomes live
@@ -1002,18 +1055,12 @@ ElimPlan::ElimPlan(const std::vector<Graph *> &graphs) : gs(graphs) {
   const int K = (int)gs.size();
   GH_CHECK(K >= 1, H2H_ERR_ARG, "no graph to contract");
   const bool force_global_stage = std::getenv("GPUH2H_GLOBAL_STAGING") != nullptr;
-  // cooperative steps keep merge buffers in shared memory only when this
-  // many warps' buffers fit, else 16 warps with buffers in global memory
-  // (GPUH2H_GRID_SMEM_WARPS; 17 = always global).  Measured on the
-  // 6.26M-vertex graph: lists of 3,456-4,264 entries left room for 5-6
-  // warps, and 16 warps staging in global memory took those levels from
-  // 212 + 480 to 194 + 403 ms; at 8 warps and above shared memory wins.
-  int grid_smem_warps = 8;
-  if (const char *e = std::getenv("GPUH2H_GRID_SMEM_WARPS")) grid_smem_warps = std::max(1, std::atoi(e));
-  // with global staging: at most this many shared-memory buffer pairs per
-  // block (GPUH2H_GRID_POOL; 0 = every merge stages in global memory)
-  int grid_pool_max = 16;
-  if (const char *e = std::getenv("GPUH2H_GRID_POOL")) grid_pool_max = std::max(0, std::min(16, std::atoi(e)));
+  // with global staging, the shared memory left over is an arena of merge
+  // buffers (GPUH2H_GRID_ARENA: 0 = every merge stages in global memory,
+  // 1 = partition levels only, 2 = the global order too)
+  int grid_arena = 2;
+  if (const char *e = std::getenv("GPUH2H_GRID_ARENA")) grid_arena = std::max(0, std::min(2, std::atoi(e)));
+
   // cell list bounds come with the elimination sets (build_elimination_sets)
   std::vector<GraphLevels> L(K);
   int threads = 1;
@@ -1177,32 +1224,21 @@ ElimPlan::ElimPlan(const std::vector<Graph *> &graphs) : gs(graphs) {
       for (int c = 0; c < ncell; c++) arrivals = std::max<int64_t>(arrivals, (int64_t)(cells[c].count + 1) * nb[c]);
       if (arrivals >= INT32_MAX) return false;  // the barrier counter compares as int
     }
-    const int64_t own = 3 * al(4LL * lmax) + 4 * al(4LL * slice_max), per_warp = 2 * al(4LL * lmax);
-    const int lal_ints = (lmax + 3) & ~3;
+    const int64_t own = 3 * al(4LL * lmax) + 4 * al(4LL * slice_max);
     if (own > smem_dyn_g) return false;
-    // per-warp merge buffers in shared memory when grid_smem_warps+ warps'
-    // worth fit (a merge walks them serially), else 16 warps with buffers in
-    // global memory
-    const int64_t fit = (smem_dyn_g - own) / per_warp;
-    const int hw = fit >= grid_smem_warps ? (int)std::min<int64_t>(16, fit) : 16;
-    const bool gstage = fit < grid_smem_warps;
-    // with global staging, the shared memory left over holds a pool of
-    // buffer pairs that merges take while one is free (near the top of the
-    // order a block runs a handful of merges per elimination): buffers of up
-    // to slot_cap entries, at least 8 of them when room allows (the lists
-    // merged there are mostly far shorter than the longest)
-    int sslots = hw, slot_cap = lal_ints;
-    if (gstage && heap) {
-      // a global order keeps the shared memory for the L1 cache: its merges
-      // read staged lists back through it (3.6M-vertex graph: 229 ms with
-      // the pool, 217 ms without)
-      sslots = 0;
-    } else if (gstage) {
-      const int64_t avail = smem_dyn_g - own;
-      slot_cap = (int)std::min<int64_t>(lal_ints, std::max<int64_t>(512, (avail / (8 * 8)) & ~int64_t(3)));
-      sslots = (int)std::min<int64_t>(std::min<int64_t>(16, avail / (8 * (int64_t)slot_cap)), grid_pool_max);
+    // 16 warps; the shared memory left over is an arena that each pick
+    // carves into the pick's hash table, the warps' match bitmaps and buffer
+    // pairs sized to the lists merged (near the top of the order a block
+    // runs a handful of merges per pick, mostly of lists far shorter than
+    // the longest); a merge that finds no room stages in global memory
+    const int hw = 16;
+    const bool gstage = true;
+    int arena = 0;
+    if (grid_arena >= (heap ? 2 : 1)) {
+      const int64_t avail = (smem_dyn_g - own) / 4;
+      if (avail >= 1024) arena = (int)(avail & ~int64_t(7));
     }
-    const int64_t hsmem = gstage ? own + (int64_t)sslots * 8 * slot_cap : own + (int64_t)hw * per_warp;
+    const int64_t hsmem = own + 4 * (int64_t)arena;
     int per = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, cell_grid_kernel, hw * 32, (size_t)hsmem) !=
             cudaSuccess ||
@@ -1223,8 +1259,7 @@ ElimPlan::ElimPlan(const std::vector<Graph *> &graphs) : gs(graphs) {
     Lc.slots = used;
     Lc.smem = hsmem;
     Lc.global_stage = gstage;
-    Lc.sslots = sslots;
-    Lc.slot_cap = slot_cap;
+    Lc.arena = arena;
     Lc.pstage_off = 0;
     Lc.grid = true;
     Lc.slice_max = slice_max;
@@ -1465,8 +1500,7 @@ void ElimPlan::launch_one(const Launch &Lc, cudaStream_t s, bool trace) {
     H.partial = (int4 *)hg_partial;
     H.bar = grid_bar + Lc.bar_off;
     H.spin_limit = spin_limit_cycles();
-    H.sslots = Lc.sslots;
-    H.slot_cap = Lc.slot_cap;
+    H.arena_ints = Lc.arena;
     cudaLaunchAttribute ca[1];
     ca[0].id = cudaLaunchAttributeCooperative;
     ca[0].val.cooperative = 1;
@@ -1487,7 +1521,7 @@ void ElimPlan::launch_one(const Launch &Lc, cudaStream_t s, bool trace) {
     float ms = 0;
     cudaEventElapsedTime(&ms, ev0, ev1);
     char pool[64] = "";
-    if (Lc.grid && Lc.global_stage) std::snprintf(pool, sizeof pool, " (pool %d x %d entries)", Lc.sslots, Lc.slot_cap);
+    if (Lc.grid && Lc.global_stage) std::snprintf(pool, sizeof pool, " (arena %d ints)", Lc.arena);
     std::fprintf(stderr,
                  "[gpuh2h] elim %s %d: %d cells x %d CTAs x %d warps, kmax %d, lmax %d, smem %lld, slots %d%s%s%s: %.3f ms\n",
                  Lc.heap ? "heap" : "level", Lc.level, Lc.ncell, Lc.cs, Lc.nw, Lc.kmax, Lc.lmax, (long long)Lc.smem,

@@ -133,7 +133,7 @@ struct Graph {
 struct ElimPlan {
   struct Launch {
     int step, level, ncell, kmax, lmax, cs, nw, slots;
-    int sslots = 0, slot_cap = 0;  // cooperative launches: shared-memory merge buffers per block, entries each
+    int arena = 0;  // cooperative launches with global staging: ints of shared-memory merge arena per block
     int64_t lo, smem, pstage_off;
     bool heap, global_stage;
     // cell_grid_kernel: the step's cells in one cooperative launch, `slots`
