@@ -616,7 +616,8 @@ struct GridArgs {
   int4 *partial;           // (deg + height, deg, id, slot) per block
   unsigned *bar;           // per cell: arrival counter
   long long spin_limit;    // bound on one barrier wait, in SM clock cycles
-  int arena_ints;          // E.pstage set: ints of shared memory that merges take buffers from, per pick
+  int arena_ints;          // ints of shared memory handed out afresh at every pick (the owned-neighbour list first)
+  int arena_merges;        // merges take their buffers from the arena (else from E.pstage)
 };
 
 __device__ __forceinline__ void better(int &bs, int &bd, int &bi, int &bp, int s, int d, int i, int p) {
@@ -699,8 +700,7 @@ __global__ void __launch_bounds__(512, 1) cell_grid_kernel(GridArgs H) {
   const int lal = (A.lmax + 3) & ~3, sal = (H.slice_max + 3) & ~3;
   int *aid = (int *)smem;
   int *aw = aid + lal;
-  int *mine = aw + lal;    // indices into aid of the neighbours this block merges
-  int *cid = mine + lal;   // the candidates this block owns: id, degree key, height key, retired
+  int *cid = aw + lal;     // the candidates this block owns: id, degree key, height key, retired
   int *cdeg = cid + sal;
   int *ch = cdeg + sal;
   int *dead = ch + sal;
@@ -716,7 +716,7 @@ __global__ void __launch_bounds__(512, 1) cell_grid_kernel(GridArgs H) {
   }
   int *const sbuf = dead + sal;
   int *const gpid = A.pstage + ((int64_t)b * nw + wid) * 2 * (int64_t)A.lmax;
-  const bool pooled = H.arena_ints > 0;
+  const bool pooled = H.arena_merges != 0;
   __shared__ int s_arena;  // pooled: arena ints taken in this pick
   Cand cand;
   cand.id = cid;
@@ -828,7 +828,11 @@ __global__ void __launch_bounds__(512, 1) cell_grid_kernel(GridArgs H) {
     __syncthreads();
     if (s_bc[3]) return;
     const int c = s_bc[2];
-    if (tid == 0) s_arena = 0;  // every merge of the last pick ended before the barrier
+    // the arena starts with this pick's list of the neighbours this block
+    // merges (indices into aid, at most c); every merge of the last pick
+    // ended before the barrier
+    int *const mine = sbuf;
+    if (tid == 0) s_arena = (c + 3) & ~3;
     // ---- the neighbours this block owns
     for (int i = tid; i < c; i += nthr)
       if (owner_of(aid[i], nb) == r) mine[atomicAdd(&s_nmine, 1)] = i;
@@ -1224,8 +1228,8 @@ ElimPlan::ElimPlan(const std::vector<Graph *> &graphs) : gs(graphs) {
       for (int c = 0; c < ncell; c++) arrivals = std::max<int64_t>(arrivals, (int64_t)(cells[c].count + 1) * nb[c]);
       if (arrivals >= INT32_MAX) return false;  // the barrier counter compares as int
     }
-    const int64_t own = 3 * al(4LL * lmax) + 4 * al(4LL * slice_max);
-    if (own > smem_dyn_g) return false;
+    const int64_t own = 2 * al(4LL * lmax) + 4 * al(4LL * slice_max);
+    if (own + al(4LL * lmax) > smem_dyn_g) return false;  // the arena holds at least the owned-neighbour list
     // 16 warps; the shared memory left over is an arena that each pick
     // carves into the pick's hash table, the warps' match bitmaps and buffer
     // pairs sized to the lists merged (near the top of the order a block
@@ -1233,11 +1237,8 @@ ElimPlan::ElimPlan(const std::vector<Graph *> &graphs) : gs(graphs) {
     // the longest); a merge that finds no room stages in global memory
     const int hw = 16;
     const bool gstage = true;
-    int arena = 0;
-    if (grid_arena >= (heap ? 2 : 1)) {
-      const int64_t avail = (smem_dyn_g - own) / 4;
-      if (avail >= 1024) arena = (int)(avail & ~int64_t(7));
-    }
+    const int arena = (int)(((smem_dyn_g - own) / 4) & ~int64_t(3));  // >= lmax ints (checked above)
+    const bool arena_merges = grid_arena >= (heap ? 2 : 1);
     const int64_t hsmem = own + 4 * (int64_t)arena;
     int per = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, cell_grid_kernel, hw * 32, (size_t)hsmem) !=
@@ -1260,6 +1261,7 @@ ElimPlan::ElimPlan(const std::vector<Graph *> &graphs) : gs(graphs) {
     Lc.smem = hsmem;
     Lc.global_stage = gstage;
     Lc.arena = arena;
+    Lc.arena_merges = arena_merges;
     Lc.pstage_off = 0;
     Lc.grid = true;
     Lc.slice_max = slice_max;
@@ -1501,6 +1503,7 @@ void ElimPlan::launch_one(const Launch &Lc, cudaStream_t s, bool trace) {
     H.bar = grid_bar + Lc.bar_off;
     H.spin_limit = spin_limit_cycles();
     H.arena_ints = Lc.arena;
+    H.arena_merges = Lc.arena_merges ? 1 : 0;
     cudaLaunchAttribute ca[1];
     ca[0].id = cudaLaunchAttributeCooperative;
     ca[0].val.cooperative = 1;
@@ -1521,7 +1524,7 @@ void ElimPlan::launch_one(const Launch &Lc, cudaStream_t s, bool trace) {
     float ms = 0;
     cudaEventElapsedTime(&ms, ev0, ev1);
     char pool[64] = "";
-    if (Lc.grid && Lc.global_stage) std::snprintf(pool, sizeof pool, " (arena %d ints)", Lc.arena);
+    if (Lc.grid) std::snprintf(pool, sizeof pool, " (arena %d ints%s)", Lc.arena, Lc.arena_merges ? "" : ", lists only");
     std::fprintf(stderr,
                  "[gpuh2h] elim %s %d: %d cells x %d CTAs x %d warps, kmax %d, lmax %d, smem %lld, slots %d%s%s%s: %.3f ms\n",
                  Lc.heap ? "heap" : "level", Lc.level, Lc.ncell, Lc.cs, Lc.nw, Lc.kmax, Lc.lmax, (long long)Lc.smem,

@@ -133,7 +133,8 @@ struct Graph {
 struct ElimPlan {
   struct Launch {
     int step, level, ncell, kmax, lmax, cs, nw, slots;
-    int arena = 0;  // cooperative launches with global staging: ints of shared-memory merge arena per block
+    int arena = 0;               // cooperative launches: ints of shared-memory arena per block
+    bool arena_merges = false;   // ... that merges take their buffers from
     int64_t lo, smem, pstage_off;
     bool heap, global_stage;
     // cell_grid_kernel: the step's cells in one cooperative launch, `slots`
