@@ -834,15 +834,43 @@ __global__ void __launch_bounds__(512, 1) cell_grid_kernel(GridArgs H) {
     if (s_bc[3]) return;
     const int c = s_bc[2];
     // the arena starts with this pick's list of the neighbours this block
-    // merges (indices into aid, at most c); every merge of the last pick
-    // ended before the barrier
+    // merges (indices into aid, at most c), then room to order them by list
+    // length; every merge of the last pick ended before the barrier
+    const int c4 = (c + 3) & ~3;
+    const bool room = 3 * c4 <= H.arena_ints;
     int *const mine = sbuf;
-    if (tid == 0) s_arena = (c + 3) & ~3;
+    int *const mlen = sbuf + c4;
+    int *const order = sbuf + 2 * c4;
+    if (tid == 0) s_arena = c4;
     // ---- the neighbours this block owns
     for (int i = tid; i < c; i += nthr)
       if (owner_of(aid[i], nb) == r) mine[atomicAdd(&s_nmine, 1)] = i;
     __syncthreads();
     const int nm = s_nmine;
+    // more merges than warps: hand them out longest list first, so a long
+    // merge does not start last (the block's merges end with its slowest
+    // warp, and the cell's step with its slowest block); the order changes
+    // no result
+    const bool lpt = room && nm > nw;
+    if (lpt) {
+      if (tid == 0) s_arena = 3 * c4;  // the merges start after the barriers below
+      for (int t = tid; t < nm; t += nthr) {
+        const int u = aid[mine[t]];
+        mlen[t] = __ldcg(A.lsize + u) - __ldcg(A.ljunk + u);
+      }
+      __syncthreads();
+      for (int t = tid; t < nm; t += nthr) {
+        const int lt = mlen[t];
+        int rk = 0;
+        for (int q = 0; q < nm; q++) {
+          const int lq = mlen[q];
+          rk += (lq > lt) || (lq == lt && q < t);
+        }
+        order[rk] = mine[t];
+      }
+      __syncthreads();
+    }
+    const int *const todo = lpt ? order : mine;
     int wbase = 0, wcap = 0;  // this warp's arena pair in this pick
     // warps take the block's neighbours one at a time as they finish, so a
     // few long lists do not hold the block (and the cell's barrier) back
@@ -851,7 +879,7 @@ __global__ void __launch_bounds__(512, 1) cell_grid_kernel(GridArgs H) {
       if (lane == 0) t = atomicAdd(&s_ntake, 1);
       t = __shfl_sync(0xffffffffu, t, 0);
       if (t >= nm) break;
-      const int i = mine[t];
+      const int i = todo[t];
       const int u = aid[i];
       const NbrMeta m = load_meta(A, u);
       if (m.s - m.J > A.lmax) {
