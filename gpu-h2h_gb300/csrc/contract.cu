@@ -1127,32 +1127,53 @@ ElimPlan::ElimPlan(const std::vector<Graph *> &graphs) : gs(graphs) {
   // slot arrays: the LUB ranges, then a pool for global-order lists that
   // outgrow theirs
   pool_size = lub + pool_extra;
-  // ---- forest arrays
-  std::vector<int64_t> f_slot_off(N);
-  std::vector<int> f_deg(N), f_cap(N), f_elim(N), f_adj_off(N + 1), f_adj_v(std::max<int64_t>(M, 1)),
+  // ---- forest arrays (written in full below, so not zero-filled first)
+  std::vector<int64_t, NoInit<int64_t>> f_slot_off(N);
+  std::vector<int, NoInit<int>> f_deg(N), f_cap(N), f_elim(N), f_adj_off(N + 1), f_adj_v(std::max<int64_t>(M, 1)),
       f_adj_w(std::max<int64_t>(M, 1)), f_heap(std::max(heap_total, 1));
+  f_adj_v[0] = f_adj_w[0] = f_heap[0] = 0;  // defined when there is nothing to copy
   {
     std::vector<int> hbase(K, 0);
     for (int i = 1; i < K; i++) hbase[i] = hbase[i - 1] + L[i - 1].heap_n;
-    Pool pool(std::min(threads, K));
-    pool.parallel_for(K, 1, [&](int64_t lo, int64_t hi, int) {
-      for (int64_t i = lo; i < hi; i++) {
-        const Graph &g = *gs[i];
-        const int vb = vbase[i];
-        for (int v = 0; v < g.n; v++) {
-          f_slot_off[vb + v] = g.slot_off[v] + lbase[i];
-          f_deg[vb + v] = g.adj_off[v + 1] - g.adj_off[v];
-          f_cap[vb + v] = g.cap[v];
-          f_elim[vb + v] = g.elim[v] + vb;
-          f_adj_off[vb + v] = g.adj_off[v] + (int)mbase[i];
-        }
-        for (int64_t e = 0; e < g.m; e++) {
-          f_adj_v[mbase[i] + e] = g.adj_v[e] + vb;
-          f_adj_w[mbase[i] + e] = g.adj_w[e];
-        }
-        for (int j = L[i].heap_start; j < g.n; j++) f_heap[hbase[i] + j - L[i].heap_start] = g.elim[j] + vb;
+    auto verts = [&](int i, int64_t lo, int64_t hi) {
+      const Graph &g = *gs[i];
+      const int vb = vbase[i];
+      for (int64_t v = lo; v < hi; v++) {
+        f_slot_off[vb + v] = g.slot_off[v] + lbase[i];
+        f_deg[vb + v] = g.adj_off[v + 1] - g.adj_off[v];
+        f_cap[vb + v] = g.cap[v];
+        f_elim[vb + v] = g.elim[v] + vb;
+        f_adj_off[vb + v] = g.adj_off[v] + (int)mbase[i];
       }
-    });
+    };
+    auto arcs = [&](int i, int64_t lo, int64_t hi) {
+      const Graph &g = *gs[i];
+      const int vb = vbase[i];
+      for (int64_t e = lo; e < hi; e++) {
+        f_adj_v[mbase[i] + e] = g.adj_v[e] + vb;
+        f_adj_w[mbase[i] + e] = g.adj_w[e];
+      }
+    };
+    auto heap = [&](int i) {
+      const Graph &g = *gs[i];
+      for (int j = L[i].heap_start; j < g.n; j++) f_heap[hbase[i] + j - L[i].heap_start] = g.elim[j] + vbase[i];
+    };
+    Pool pool(threads);
+    if (K >= threads) {  // a batch: a graph per task
+      pool.parallel_for(K, 1, [&](int64_t lo, int64_t hi, int) {
+        for (int64_t i = lo; i < hi; i++) {
+          verts((int)i, 0, gs[i]->n);
+          arcs((int)i, 0, gs[i]->m);
+          heap((int)i);
+        }
+      });
+    } else {  // few graphs: ranges of each graph's vertices and arcs per task
+      for (int i = 0; i < K; i++) {
+        pool.parallel_for(gs[i]->n, 1 << 16, [&](int64_t lo, int64_t hi, int) { verts(i, lo, hi); });
+        pool.parallel_for(gs[i]->m, 1 << 17, [&](int64_t lo, int64_t hi, int) { arcs(i, lo, hi); });
+        heap(i);
+      }
+    }
   }
   f_adj_off[N] = (int)M;
   // ---- launches.  Step s takes level H_i - s of every graph still above
@@ -1627,10 +1648,13 @@ void ElimPlan::check_error() {
 }
 
 void ElimPlan::build_lists() {
-  std::vector<int> f_lsize(N), f_elim(N), f_father(N);
+  int threads = 1;
+  for (const Graph *g : gs) threads = std::max(threads, g->threads);
+  Pool pool(threads);
+  std::vector<int, NoInit<int>> f_lsize(N), f_elim(N), f_father(N);
   GH_CUDA(cudaMemcpy(f_lsize.data(), lsize, sizeof(int) * N, cudaMemcpyDeviceToHost));
-  std::vector<int64_t> off(N + 1, 0);
-  for (int v = 0; v < N; v++) off[v + 1] = off[v] + f_lsize[v];
+  std::vector<int64_t, NoInit<int64_t>> off(N + 1);
+  parallel_prefix(pool, N, off.data(), [&](int64_t v) { return (int64_t)f_lsize[v]; });
   const int64_t tot = off[N];
   auto la = std::make_shared<ListArrays>();
   la->off = dalloc<int64_t>(N + 1);
@@ -1654,11 +1678,16 @@ void ElimPlan::build_lists() {
   for (size_t i = 0; i < gs.size(); i++) {
     Graph &g = *gs[i];
     const int vb = vbase[i];
-    for (int v = 0; v < g.n; v++) g.elim[v] = f_elim[vb + v] - vb;
-    g.father.assign(g.n, -1);
-    for (int v = 0; v < g.n; v++) g.father[v] = f_father[vb + v] < 0 ? -1 : f_father[vb + v] - vb;
-    g.x_off.assign(g.n + 1, 0);
-    for (int v = 0; v < g.n; v++) g.x_off[v + 1] = g.x_off[v] + f_lsize[vb + v];
+    g.father.resize(g.n);
+    g.x_off.resize(g.n + 1);
+    pool.parallel_for(g.n, 1 << 16, [&](int64_t lo, int64_t hi, int) {
+      for (int64_t v = lo; v < hi; v++) {
+        g.elim[v] = f_elim[vb + v] - vb;
+        g.father[v] = f_father[vb + v] < 0 ? -1 : f_father[vb + v] - vb;
+        g.x_off[v + 1] = off[vb + v + 1] - off[vb];
+      }
+    });
+    g.x_off[0] = 0;
     g.decomposition_size = g.x_off[g.n] + g.n;
     std::vector<int>().swap(g.x_id);
     std::vector<int>().swap(g.x_w);
