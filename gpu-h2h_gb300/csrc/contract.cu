@@ -862,9 +862,9 @@ __global__ void __launch_bounds__(512, 1) cell_grid_kernel(GridArgs H) {
       for (int t = tid; t < nm; t += nthr) {
         const int lt = mlen[t];
         int rk = 0;
-        for (int q = 0; q < nm; q++) {
-          const int lq = mlen[q];
-          rk += (lq > lt) || (lq == lt && q < t);
+        for (int o = 0; o < nm; o++) {
+          const int lo = mlen[o];
+          rk += (lo > lt) || (lo == lt && o < t);
         }
         order[rk] = mine[t];
       }
