@@ -217,14 +217,17 @@ __device__ __forceinline__ NbrMeta load_meta(const ElimArgs &A, int u) {
 // near the top of the order lists hold thousands of entries and the load is
 // the merge's latency.  The slot arrays are padded by four entries, so a
 // vector that starts inside the list never leaves the allocation.
+// u's list minus v (P) into pid/pw by one warp; returns |P| in every lane.
+// kWide: 128-bit loads, four per lane in flight (2 KB of ids and 2 KB of
+// weights per warp per round trip instead of 512 B each); the slot arrays
+// are padded by four entries, so a vector that starts inside the list never
+// leaves the allocation.
 template <bool kWide>
-__device__ __forceinline__ void merge_neighbour(const ElimArgs &A, int u, const NbrMeta &m, int wu, int iu, int v, int hnow,
-                                const int *aid, const int *aw, int c, int *pid, int *pw, int lane, Cand cand,
-                                int nslots) {
-  int64_t off = m.off;
+__device__ __forceinline__ int load_p(const ElimArgs &A, const NbrMeta &m, int v, int *pid, int *pw, int lane) {
+  int np = 0;
+  const int64_t off = m.off;
   const int s = m.s;
   const int J = m.J;
-  int np = 0;
   if (kWide) {
     const int64_t lo = off + J, hi = off + s;
     for (int64_t base = lo & ~int64_t(3); base < hi; base += 4 * 32 * 4) {
@@ -293,12 +296,47 @@ __device__ __forceinline__ void merge_neighbour(const ElimArgs &A, int u, const 
     }
   }
   __syncwarp();
+  return np;
+}
+
+//
+// kTeam: T warps (tw = this warp's place among them) share the merge: the
+// first stages P, then the merge path is cut into 32*T stretches, one per
+// lane of the team, with a prefix of the warps' counts over `tsh` (12 ints
+// of shared memory per team) and named barrier `bid` over the team's 32*T
+// threads.  Every warp of the team takes the same branches (all depend on
+// values the team shares), so each reaches every barrier.
+template <bool kWide, bool kTeam = false>
+__device__ __forceinline__ void merge_neighbour(const ElimArgs &A, int u, const NbrMeta &m, int wu, int iu, int v, int hnow,
+                                const int *aid, const int *aw, int c, int *pid, int *pw, int lane, Cand cand,
+                                int nslots, int T = 1, int tw = 0, int bid = 0, int *tsh = nullptr) {
+  auto tsync = [&]() {
+    if (kTeam)
+      asm volatile("bar.sync %0, %1;" ::"r"(bid), "r"(32 * T) : "memory");
+    else
+      __syncwarp();
+  };
+  int64_t off = m.off;
+  const int s = m.s;
+  const int J = m.J;
+  int np;
+  if (kTeam) {
+    if (tw == 0) {
+      const int n0 = load_p<kWide>(A, m, v, pid, pw, lane);
+      if (lane == 0) tsh[0] = n0;
+    }
+    tsync();
+    np = tsh[0];
+  } else {
+    np = load_p<kWide>(A, m, v, pid, pw, lane);
+  }
+  const int L = kTeam ? 32 * T : 32, tl = kTeam ? 32 * tw + lane : lane;  // stretches, this lane's
   const int nq = c - 1;
   // nothing valid left: the partition kernel keeps its stale size, a heap map is empty
   const int Jn = (np > 0 || A.heap_mode) ? 0 : s;
   const int total_len = np + nq;
-  const int seg = (total_len + 31) >> 5;
-  const int k0 = min(lane * seg, total_len), k1 = min(k0 + seg, total_len);
+  const int seg = (total_len + L - 1) / L;
+  const int k0 = min(tl * seg, total_len), k1 = min(k0 + seg, total_len);
   const int i0 = corank(pid, np, aid, iu, nq, k0);
   const int plast = max(0, np - 1), qlast = max(0, nq - 1);  // clamped load indices (in bounds when empty)
   // pass 1: count outputs, apply matched updates to the first entry of the
@@ -345,7 +383,19 @@ __device__ __forceinline__ void merge_neighbour(const ElimArgs &A, int u, const 
     const int y = __shfl_up_sync(0xffffffffu, incl, o);
     if (lane >= o) incl += y;
   }
-  const int total = __shfl_sync(0xffffffffu, incl, 31);
+  int total, before = 0;  // outputs of the merge, of the team's warps before this one
+  if (kTeam) {
+    if (lane == 31) tsh[1 + tw] = incl;
+    tsync();  // also orders pass 1's updates before pass 2's reads across the team
+    total = 0;
+    for (int w = 0; w < T; w++) {
+      const int x = tsh[1 + w];
+      before += w < tw ? x : 0;
+      total += x;
+    }
+  } else {
+    total = __shfl_sync(0xffffffffu, incl, 31);
+  }
   const int capu = m.cap;
   bool fits = Jn + total <= capu;
   if (!fits && A.heap_mode) {
@@ -353,15 +403,24 @@ __device__ __forceinline__ void merge_neighbour(const ElimArgs &A, int u, const 
     // list to a fresh range (the merge writes a full new copy anyway)
     int64_t fresh = -1;
     const int ncap = max(2 * capu, Jn + total);
-    if (lane == 0) {
+    if (tl == 0) {
       const unsigned long long at = atomicAdd(A.pool_next, (unsigned long long)ncap);
       if ((int64_t)at + ncap <= A.pool_size) fresh = (int64_t)at;
     }
-    fresh = __shfl_sync(0xffffffffu, fresh, 0);
+    if (kTeam) {
+      if (tl == 0) {
+        tsh[6] = (int)(fresh & 0xffffffffll);
+        tsh[7] = (int)(fresh >> 32);
+      }
+      tsync();
+      fresh = (int64_t)(((uint64_t)(unsigned)tsh[7] << 32) | (unsigned)tsh[6]);
+    } else {
+      fresh = __shfl_sync(0xffffffffu, fresh, 0);
+    }
     if (fresh >= 0) {
       off = fresh;
       fits = true;
-      if (lane == 0) {
+      if (tl == 0) {
         A.slot_off[u] = fresh;
         A.cap[u] = ncap;
       }
@@ -371,14 +430,14 @@ __device__ __forceinline__ void merge_neighbour(const ElimArgs &A, int u, const 
     // no insert (every member of Q is already in P, as near the top of the
     // order): the output is P with its matched entries min-updated, written
     // contiguously
-    for (int k = lane; k < np; k += 32) {
+    for (int k = tl; k < np; k += L) {
       A.slot_nbr[off + k] = pid[k];
       A.slot_w[off + k] = pw[k];
     }
   } else if (fits) {
     // pass 2, branch-free as pass 1: write P's entries and the unmatched Q
     // entries of this lane's stretch
-    int o = incl - cnt;
+    int o = before + incl - cnt;
     int i = i0, j = k0 - i0;
     int a = i < np ? pid[i] : INT_MAX;
     int b = j < nq ? q_at(aid, iu, j) : INT_MAX;
@@ -400,9 +459,9 @@ __device__ __forceinline__ void merge_neighbour(const ElimArgs &A, int u, const 
       a = i < np ? na : INT_MAX;
       b = j < nq ? nb : INT_MAX;
     }
-    for (int k = lane; k < Jn; k += 32) A.slot_nbr[off + k] = INT_MAX;
+    for (int k = tl; k < Jn; k += L) A.slot_nbr[off + k] = INT_MAX;
   }
-  if (lane == 0) {
+  if (tl == 0) {
     if (!fits) set_err(A.err, kErrOverflow);
     const int ns = fits ? Jn + total : s;
     A.lsize[u] = ns;
@@ -416,7 +475,7 @@ __device__ __forceinline__ void merge_neighbour(const ElimArgs &A, int u, const 
       cand.third[p] = hn;
     }
   }
-  __syncwarp();
+  tsync();  // the buffers are free again
 }
 
 // 48 registers: five 8-warp CTAs per SM for the many small cells at the
@@ -723,6 +782,7 @@ __global__ void __launch_bounds__(512, 1) cell_grid_kernel(GridArgs H) {
   int *const gpid = A.pstage + ((int64_t)b * nw + wid) * 2 * (int64_t)A.lmax;
   const bool pooled = H.arena_merges != 0;
   __shared__ int s_arena;  // pooled: arena ints taken in this pick
+  __shared__ int s_team[16 * 12];  // per warp team: merge_neighbour's exchange, then the team's pair and ticket
   Cand cand;
   cand.id = cid;
   cand.deg = cdeg;
@@ -871,10 +931,66 @@ __global__ void __launch_bounds__(512, 1) cell_grid_kernel(GridArgs H) {
       __syncthreads();
     }
     const int *const todo = lpt ? order : mine;
+    // fewer merges than a quarter (a half) of the warps, as in a global
+    // order: teams of 4 (2) warps share each merge, so the step's longest
+    // merge runs on more lanes (team size, like nm, is the same in every warp
+    // of the block)
+    const int T = !pooled ? 1 : 4 * nm <= nw ? 4 : 2 * nm <= nw ? 2 : 1;
+    if (T > 1) {
+      const int team = wid / T, tw = wid - team * T, bid = 1 + team;
+      int *const tsh = s_team + 12 * team;
+      int *const tg = A.pstage + ((int64_t)b * nw + team * T) * 2 * (int64_t)A.lmax;  // the first warp's slab
+      int tbase = 0, tcap = 0;  // the team's arena pair, held by its first warp
+      for (;;) {
+        // the first warp takes the ticket and, when the list outgrows the
+        // team's pair, a new pair from the arena; the team reads both after
+        // the barrier
+        if (tw == 0) {
+          int t = 0;
+          if (lane == 0) t = atomicAdd(&s_ntake, 1);
+          t = __shfl_sync(0xffffffffu, t, 0);
+          if (t < nm) {
+            const int u = aid[todo[t]];
+            const int len = __ldcg(A.lsize + u) - __ldcg(A.ljunk + u);
+            if (len <= A.lmax && len > tcap) {
+              const int want = (len + 3) & ~3;
+              const int at = arena_take(&s_arena, H.arena_ints, 2 * want, lane);
+              if (at >= 0) {
+                tbase = at;
+                tcap = want;
+              }
+            }
+          }
+          if (lane == 0) {
+            tsh[8] = tbase;
+            tsh[9] = tcap;
+            tsh[10] = t;
+          }
+        }
+        asm volatile("bar.sync %0, %1;" ::"r"(bid), "r"(32 * T) : "memory");
+        const int t = tsh[10], sb = tsh[8], scp = tsh[9];
+        if (t >= nm) break;
+        const int i = todo[t];
+        const int u = aid[i];
+        const NbrMeta m = load_meta(A, u);
+        if (m.s - m.J > A.lmax) {  // the same m in every warp of the team
+          if (tw == 0 && lane == 0) set_err(A.err, kErrStaging);
+          // every warp has read the ticket before the first warp takes the next
+          asm volatile("bar.sync %0, %1;" ::"r"(bid), "r"(32 * T) : "memory");
+          continue;
+        }
+        if (m.s - m.J <= scp)
+          merge_neighbour<true, true>(A, u, m, aw[i], i, v, hnow, aid, aw, c, sbuf + sb, sbuf + sb + scp, lane, cand,
+                                      ns, T, tw, bid, tsh);
+        else
+          merge_neighbour<true, true>(A, u, m, aw[i], i, v, hnow, aid, aw, c, tg, tg + A.lmax, lane, cand, ns, T, tw,
+                                      bid, tsh);
+      }
+    }
     int wbase = 0, wcap = 0;  // this warp's arena pair in this pick
     // warps take the block's neighbours one at a time as they finish, so a
     // few long lists do not hold the block (and the cell's barrier) back
-    for (;;) {
+    for (; T == 1;) {
       int t = 0;
       if (lane == 0) t = atomicAdd(&s_ntake, 1);
       t = __shfl_sync(0xffffffffu, t, 0);

@@ -187,15 +187,18 @@ def test_global_merge_staging(cfg0_root, golden0, monkeypatch):
         assert np.array_equal(_sha(g.labels()["dis"]), golden0[tag + "sha256/dis"])
 
 
-@pytest.mark.parametrize("env,value", [("GPUH2H_CLUSTER_HEAP", "1"), ("GPUH2H_GRID_CELLS", "100000"),
-                                       ("GPUH2H_LEVEL_FILL", "1")])
-def test_alternate_kernels(cfg0_root, golden0, monkeypatch, env, value):
+@pytest.mark.parametrize("envs", [{"GPUH2H_CLUSTER_HEAP": "1"}, {"GPUH2H_GRID_CELLS": "100000"},
+                                  {"GPUH2H_GRID_CELLS": "100000", "GPUH2H_GRID_ARENA": "0"},
+                                  {"GPUH2H_LEVEL_FILL": "1"}])
+def test_alternate_kernels(cfg0_root, golden0, monkeypatch, envs):
     """Every elimination step on thread-block clusters (no cooperative
     launch), every step as one cooperative launch over all SMs (partition
-    cells included), and the level-synchronous L4 fill (instead of the
+    cells included) with merge buffers from the shared-memory arena or all
+    in global memory, and the level-synchronous L4 fill (instead of the
     dataflow) give the same order, adjacency, labels and answers."""
     import gpuh2h
-    monkeypatch.setenv(env, value)
+    for env, value in envs.items():
+        monkeypatch.setenv(env, value)
     for C in (1, 2, 6):
         tag = "cfg0_C%d_L4/" % C
         g = build(gpuh2h.files_for(cfg0_root, "cfg0"), 6, C)
