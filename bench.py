@@ -521,6 +521,35 @@ def cpu_baseline_run(threads: int, budget_s: float) -> dict:
     return dict(contract_s=t1 - t0, labels_s=t2 - t1, query_s=q_time, queries=done, reps=reps, nq=len(x))
 
 
+def plain_gpu_reference_run(threads: int) -> dict:
+    """The reference's own GPU path beside this library's: its unmodified G2H
+    command line, built for sm_103a from the staged sources
+    (oracle/build_ref_gpu.sh), and this library's G2H, both as
+    `G2H cfg0 6 1 T 1 1 2 1` on the same seeded 4,096-vertex graph, each run
+    timed by its own CSV timers (microseconds): TDInGPUTime = partition
+    contraction, TDInCPUTime = global order, H2HUsingTime_GPU = GPU label fill
+    (the shipped L3 labels), GPU*-256 = one batch of 1e6 uniform pairs.  The
+    larger graphs are beyond it: it contracts each cell with one GPU thread
+    that bubble-sorts the cell before every pick, cubic in a cell's size."""
+    from gpuh2h import _build
+
+    from oracle import oracle
+    from oracle import plain_gpu_reference as pgr
+    if not oracle.build_ref_gpu():
+        return {"unavailable": "the reference's sources are not staged on this machine"}
+    import gpuh2h
+    params, H, C = pgr.GRAPHS["cfg0"]
+    with tempfile.TemporaryDirectory() as rr, tempfile.TemporaryDirectory() as ro:
+        oracle.generate_road(rr, "cfg0", **params)
+        gpuh2h.generate_road(ro, "cfg0", **params)
+        env = dict(os.environ)
+        ref = pgr.run_cli(os.path.join(pgr.HERE, "_ref", "G2H_ref"), rr, "cfg0", H, C, threads, env)
+        ours = pgr.run_cli(_build.CLI, ro, "cfg0", H, C, threads, dict(env, H2H_LABEL="L3"))
+    return {"graph": "cfg0 (4,096 vertices, H=6, C=1)", "reference": ref, "ours": ours,
+            "what": "the reference's unmodified G2H (nvcc sm_103a) and this library's G2H, same graph and "
+                    "arguments `G2H cfg0 6 1 T 1 1 2 1`; microseconds from each run's own CSV timers"}
+
+
 def files_for(root: str, name: str):
     pre = os.path.join(root, "Partition", name, "Latitude")
     return (os.path.join(root, "Graph", "USA", name + "Edge.txt"), pre + "ID.txt", pre + "Cut.txt")
@@ -826,6 +855,10 @@ def main():
                          "+ labels %.1f s)" % (CPU_WORKLOAD, cb["reps"], cb["nq"], cores,
                                                cb["contract_s"] + cb["labels_s"], cb["contract_s"], cb["labels_s"]),
                "build_s": cb["contract_s"] + cb["labels_s"]}
+    # ---- the reference's own GPU path on the graph it can contract in seconds
+    plain_ref = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline and not args.no_extras:
+        plain_ref = plain_gpu_reference_run(os.cpu_count() or 1)
     line = {
         "metric": METRIC, "value": value, "unit": "queries/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1000.0 * t_max / args.steps, "higher_is_better": True,
@@ -848,6 +881,7 @@ def main():
         "clocks": clocks,
         "parity": parity,
         "cpu_baseline": cpu,
+        "plain_gpu_reference": plain_ref,
     }
     line.update(extras)
     if rank == 0:
