@@ -9,8 +9,9 @@ t within 20 hops of s) answered in UsingLCA mode on the device-resident index.
 The line also carries the build (phases), p50/p99 of 10^5-pair batches alone
 and with four in flight through the continuous-batching server, e2e through
 the host-buffer C ABI call, a Dijkstra check of sampled sources against every
-target, and -- as extra keys -- the 264,346-vertex graph and the 64-graph
-batched build.
+target, and -- as extra keys -- the 264,346-vertex graph, the 64-graph
+batched build and the reference's own GPU command line timed beside this
+library's on the 4,096-vertex graph.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
                   [--workload road6m|cfg1|road3m] [--serve]
