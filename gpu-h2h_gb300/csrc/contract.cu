@@ -682,6 +682,8 @@ struct GridArgs {
   long long spin_limit;    // bound on one barrier wait, in SM clock cycles
   int arena_ints;          // ints of shared memory handed out afresh at every pick (the owned-neighbour list first)
   int arena_merges;        // merges take their buffers from the arena (else from E.pstage)
+  unsigned *done_cnt;      // per block: merges of the neighbours it owns finished in this pick (balance)
+  int balance;             // split each pick's merges over the cell's blocks by work, not by owner
 };
 
 __device__ __forceinline__ void better(int &bs, int &bd, int &bi, int &bp, int s, int d, int i, int p) {
@@ -893,18 +895,45 @@ __global__ void __launch_bounds__(512, 1) cell_grid_kernel(GridArgs H) {
     __syncthreads();
     if (s_bc[3]) return;
     const int c = s_bc[2];
+    // balance: block r merges v's neighbours [r c / nb, (r + 1) c / nb) --
+    // the same split in every block, from c and nb alone (the list sizes
+    // change under other blocks' merges, so they cannot set it) -- and a
+    // merge of a neighbour owned by another block counts on that owner's
+    // counter; each owner takes its candidates' keys from the merged lists
+    // once its count is in.  Every block then has c / nb merges, few enough
+    // in a global order for warp teams.  Only cells of 16 or more blocks:
+    // on fewer (the partition levels of many cells) the owners' waits cost
+    // more than the split gains.  Otherwise a block merges the neighbours
+    // it owns.
+    const bool bal = H.balance != 0 && nb >= 16;
+    int lo_r = 0, hi_r = 0, cnt_own = 0;
+    if (bal) {
+      lo_r = (int)((int64_t)r * c / nb);
+      hi_r = (int)((int64_t)(r + 1) * c / nb);
+      int own = 0;
+      for (int i = tid; i < c; i += nthr) own += owner_of(aid[i], nb) == r;
+      for (int o = 16; o > 0; o >>= 1) own += __shfl_xor_sync(0xffffffffu, own, o);
+      if (lane == 0) s_rd[wid] = own;
+      __syncthreads();
+      for (int w = 0; w < nw; w++) cnt_own += s_rd[w];
+    }
     // the arena starts with this pick's list of the neighbours this block
     // merges (indices into aid, at most c), then room to order them by list
     // length; every merge of the last pick ended before the barrier
     const int c4 = (c + 3) & ~3;
     const bool room = 3 * c4 <= H.arena_ints;
     int *const mine = sbuf;
-    int *const mlen = sbuf + c4;
-    int *const order = sbuf + 2 * c4;
+    int *const mlen = mine + c4;
+    int *const order = mine + 2 * c4;
     if (tid == 0) s_arena = c4;
-    // ---- the neighbours this block owns
-    for (int i = tid; i < c; i += nthr)
-      if (owner_of(aid[i], nb) == r) mine[atomicAdd(&s_nmine, 1)] = i;
+    // ---- the neighbours this block merges
+    if (bal) {
+      for (int t = tid; t < hi_r - lo_r; t += nthr) mine[t] = lo_r + t;
+      if (tid == 0) s_nmine = hi_r - lo_r;
+    } else {
+      for (int i = tid; i < c; i += nthr)
+        if (owner_of(aid[i], nb) == r) mine[atomicAdd(&s_nmine, 1)] = i;
+    }
     __syncthreads();
     const int nm = s_nmine;
     // more merges than warps: hand them out longest list first, so a long
@@ -915,7 +944,7 @@ __global__ void __launch_bounds__(512, 1) cell_grid_kernel(GridArgs H) {
     if (lpt) {
       if (tid == 0) s_arena = 3 * c4;  // the merges start after the barriers below
       for (int t = tid; t < nm; t += nthr) {
-        const int u = aid[mine[t]];
+        const int u = aid[mine[t]];  // merged by this block alone: its size is this pick's
         mlen[t] = __ldcg(A.lsize + u) - __ldcg(A.ljunk + u);
       }
       __syncthreads();
@@ -979,12 +1008,17 @@ __global__ void __launch_bounds__(512, 1) cell_grid_kernel(GridArgs H) {
           asm volatile("bar.sync %0, %1;" ::"r"(bid), "r"(32 * T) : "memory");
           continue;
         }
+        // balance: the owner takes the keys from the merged list (nslots 0)
         if (m.s - m.J <= scp)
           merge_neighbour<true, true>(A, u, m, aw[i], i, v, hnow, aid, aw, c, sbuf + sb, sbuf + sb + scp, lane, cand,
-                                      ns, T, tw, bid, tsh);
+                                      bal ? 0 : ns, T, tw, bid, tsh);
         else
-          merge_neighbour<true, true>(A, u, m, aw[i], i, v, hnow, aid, aw, c, tg, tg + A.lmax, lane, cand, ns, T, tw,
-                                      bid, tsh);
+          merge_neighbour<true, true>(A, u, m, aw[i], i, v, hnow, aid, aw, c, tg, tg + A.lmax, lane, cand,
+                                      bal ? 0 : ns, T, tw, bid, tsh);
+        if (bal && tw == 0 && lane == 0) {  // the team's writes precede (the merge ends at a team barrier)
+          __threadfence();
+          atomicAdd(H.done_cnt + f + owner_of(u, nb), 1u);
+        }
       }
     }
     int wbase = 0, wcap = 0;  // this warp's arena pair in this pick
@@ -1021,11 +1055,47 @@ __global__ void __launch_bounds__(512, 1) cell_grid_kernel(GridArgs H) {
         }
       }
       if (in_smem)
-        merge_neighbour<true>(A, u, m, aw[i], i, v, hnow, aid, aw, c, sp, sp + scap, lane, cand, ns);
+        merge_neighbour<true>(A, u, m, aw[i], i, v, hnow, aid, aw, c, sp, sp + scap, lane, cand, bal ? 0 : ns);
       else
-        merge_neighbour<true>(A, u, m, aw[i], i, v, hnow, aid, aw, c, gpid, gpid + A.lmax, lane, cand, ns);
+        merge_neighbour<true>(A, u, m, aw[i], i, v, hnow, aid, aw, c, gpid, gpid + A.lmax, lane, cand,
+                              bal ? 0 : ns);
+      if (bal && lane == 0) {  // the warp's writes precede (the merge ends at __syncwarp)
+        __threadfence();
+        atomicAdd(H.done_cnt + f + owner_of(u, nb), 1u);
+      }
     }
     __syncthreads();
+    if (bal) {
+      // every merge of a neighbour this block owns is done once its count is
+      // in (every block merges its range before it waits here, so the waits
+      // end); then the keys of its candidates among v's neighbours come from
+      // the sizes and heights those merges wrote, and the count is cleared
+      // for the next pick (the next increments follow the cell barrier)
+      if (tid == 0) {
+        unsigned *const cnt = H.done_cnt + b;
+        const long long t0 = clock64();
+        int ok = 1;
+        while ((int)(ld_acquire_u32(cnt) - (unsigned)cnt_own) < 0) {
+          if (*(volatile int *)A.err != 0) { ok = 0; break; }
+          if (clock64() - t0 > H.spin_limit) { set_err(A.err, kErrTimeout); ok = 0; break; }
+        }
+        *cnt = 0u;
+        s_flag = ok;
+      }
+      __syncthreads();
+      if (!s_flag) return;
+      for (int i = tid; i < c; i += nthr) {
+        const int u = aid[i];
+        if (owner_of(u, nb) == r) {
+          const int p = __ldcg(A.cpos + u);
+          if (p >= 0 && p < ns) {
+            cdeg[p] = __ldcg(A.lsize + u);
+            ch[p] = __ldcg(A.height + u);
+          }
+        }
+      }
+      __syncthreads();
+    }
     // ---- after the first pick of a partition cell every key becomes live
     // (kernel_functions.cu:471-475); this block alone wrote its candidates' lists
     if (j == 0 && !A.heap_mode) {
@@ -1213,6 +1283,9 @@ ElimPlan::ElimPlan(const std::vector<Graph *> &graphs) : gs(graphs) {
   // 1 = partition levels only, 2 = the global order too)
   int grid_arena = 2;
   if (const char *e = std::getenv("GPUH2H_GRID_ARENA")) grid_arena = std::max(0, std::min(2, std::atoi(e)));
+  // cooperative steps: split each pick's merges over the cell's blocks by
+  // work (GPUH2H_ELIM_BALANCE=0: each block merges the neighbours it owns)
+  if (const char *e = std::getenv("GPUH2H_ELIM_BALANCE")) elim_balance = std::atoi(e) != 0;
 
   // cell list bounds come with the elimination sets (build_elimination_sets)
   std::vector<GraphLevels> L(K);
@@ -1573,7 +1646,8 @@ ElimPlan::ElimPlan(const std::vector<Graph *> &graphs) : gs(graphs) {
     heap_verts = palloc<int>(std::max(heap_total, 1), bytes);
     if (pstage_ints) pstage = palloc<int>(pstage_ints, bytes);
     if (!gmap.empty()) {
-      hg_partial = palloc<int4>(partial_max, bytes);
+      hg_partial = palloc<int4>(2 * partial_max, bytes);  // per block: argmin, then (first word) merge count
+      partial_cap = partial_max;
       grid_map = palloc<int>(gmap.size(), bytes);
       grid_bar = palloc<unsigned>(grid_bar_words, bytes);
       GH_CUDA(cudaMemcpy(grid_map, gmap.data(), sizeof(int) * gmap.size(), cudaMemcpyHostToDevice));
@@ -1674,6 +1748,9 @@ void ElimPlan::launch_one(const Launch &Lc, cudaStream_t s, bool trace) {
     H.spin_limit = spin_limit_cycles();
     H.arena_ints = Lc.arena;
     H.arena_merges = Lc.arena_merges ? 1 : 0;
+    H.done_cnt = reinterpret_cast<unsigned *>((int4 *)hg_partial + partial_cap);
+    H.balance = elim_balance ? 1 : 0;
+    GH_CUDA(cudaMemsetAsync(H.done_cnt, 0, sizeof(unsigned) * Lc.slots, s));
     cudaLaunchAttribute ca[1];
     ca[0].id = cudaLaunchAttributeCooperative;
     ca[0].val.cooperative = 1;

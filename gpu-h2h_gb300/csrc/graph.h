@@ -152,6 +152,8 @@ struct ElimPlan {
   int64_t M = 0, lub = 0, pool_size = 0;
   std::vector<Launch> launches;  // in step order; launches of one step are independent
   int nsm = 0, max_group = 1;
+  bool elim_balance = true;  // cooperative steps: merges split over a cell's blocks by work
+  int64_t partial_cap = 0;   // blocks the per-block arrays of cooperative launches hold
   std::vector<cudaStream_t> side;  // streams for the second and later launches of a step
   std::vector<cudaEvent_t> ev_join;
   cudaEvent_t ev_fork = nullptr;
