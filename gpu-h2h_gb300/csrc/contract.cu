@@ -901,11 +901,12 @@ __global__ void __launch_bounds__(512, 1) cell_grid_kernel(GridArgs H) {
     // merge of a neighbour owned by another block counts on that owner's
     // counter; each owner takes its candidates' keys from the merged lists
     // once its count is in.  Every block then has c / nb merges, few enough
-    // in a global order for warp teams.  Only cells of 16 or more blocks:
-    // on fewer (the partition levels of many cells) the owners' waits cost
-    // more than the split gains.  Otherwise a block merges the neighbours
-    // it owns.
-    const bool bal = H.balance != 0 && nb >= 16;
+    // in a global order for warp teams.  Only cells of 16 or more blocks
+    // and picks with at least two merges per block: elsewhere (the partition
+    // levels of many cells, the short lists of a small graph's global order)
+    // the owners' waits cost more than the split gains.  Otherwise a block
+    // merges the neighbours it owns.
+    const bool bal = H.balance != 0 && nb >= 16 && c >= 2 * nb;
     int lo_r = 0, hi_r = 0, cnt_own = 0;
     if (bal) {
       lo_r = (int)((int64_t)r * c / nb);
