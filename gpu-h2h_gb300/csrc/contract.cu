@@ -652,19 +652,25 @@ __global__ void __maxnreg__(48) elim_kernel(ElimArgs A) {
 // eliminations whose neighbour merges want more SMs than that.
 //
 // Ownership: block r of a cell's nb blocks owns the vertices u with
-// owner_of(u, nb) == r (a scrambled id mod nb).  It keeps the keys of the candidates it owns in shared
-// memory (their slots in cpos), merges the lists of the neighbours it owns
-// (candidates or not), refreshes their keys and retires its picked
-// candidate.  So a block finds its share of v's neighbours without a memory
-// round trip, and the argmin of its candidates reads only shared memory.
+// owner_of(u, nb) == r (a scrambled id mod nb).  It keeps the keys of the
+// candidates it owns in shared memory (their slots in cpos), refreshes their
+// keys and retires its picked candidate; the argmin of its candidates reads
+// only shared memory.
 // Per elimination:
 //   every block of the cell reduces the cell's per-block argmins to the same
 //   pick v (the key order is strict; the pick's height is its sum minus its
 //   degree); the first block records it and writes back the previous pick's
 //   compacted list (nobody reads that list any more); every block loads and
 //   compacts v's list into its shared memory (the same code as the cluster
-//   leader), merges the neighbours of v it owns, and publishes the argmin of
-//   its candidates                                          -- cell barrier
+//   leader) and merges a share of v's neighbours: the ones it owns (their
+//   keys updated in place), or -- in cells of 16+ blocks with at least two
+//   merges per block -- an even range of v's list, a merge of a neighbour
+//   owned elsewhere counting on the owner's counter, each owner waiting for
+//   its count and then taking its candidates' keys from the merged lists;
+//   then it publishes the argmin of its candidates            -- cell barrier
+// Within a block, warps take merges from a shared counter (longest list
+// first when they outnumber the warps, or teams of 2-4 warps per merge when
+// they are few), with buffers cut from a shared-memory arena per pick.
 // The cell barrier is a monotonic arrival counter in global memory (barrier
 // t completes when it reaches t * nb); the launch is cooperative, so every
 // block is resident, and a wait is bounded (the block records kErrTimeout and
