@@ -774,8 +774,9 @@ FillPlan::FillPlan(const std::vector<Graph *> &graphs, const TilePolicy &pol, co
     dis_total += gdis[i];
     max_m = std::max(max_m, gmax_m[i]);
   }
-  std::vector<int64_t> f_drow(N + 1, 0), f_pos_hash(N + 1, 0);
-  std::vector<int> f_father(N), f_depth(N), f_hld(N);
+  // forest arrays, every entry written below (so not zero-filled first)
+  std::vector<int64_t, NoInit<int64_t>> f_drow(N + 1), f_pos_hash(N + 1);
+  std::vector<int, NoInit<int>> f_father(N), f_depth(N), f_hld(N);
   std::vector<int64_t> sbase(K, 0);
   int64_t seg_total = 0;
   for (int i = 0; i < K; i++) {
@@ -783,8 +784,8 @@ FillPlan::FillPlan(const std::vector<Graph *> &graphs, const TilePolicy &pol, co
     seg_total += gs[i]->seg_off[gs[i]->n];
     max_segs = std::max(max_segs, gs[i]->max_segs);
   }
-  std::vector<int64_t> f_seg_off(N + 1, 0);
-  std::vector<int> f_htop(N), f_hpos(N);
+  std::vector<int64_t, NoInit<int64_t>> f_seg_off(N + 1);
+  std::vector<int, NoInit<int>> f_htop(N), f_hpos(N);
   pool.parallel_for(nvr, 1, [&](int64_t lo, int64_t hi, int) {
     for (int64_t r = lo; r < hi; r++) {
       const int i = vr[r].g;
@@ -993,7 +994,7 @@ void FillPlan::build_tiles(const TilePolicy &pol) {
   // per item, staging bounds
   const std::vector<LevelItem> items = level_items(gs);
   const int64_t nitems = (int64_t)items.size();
-  std::vector<int> host((size_t)4 * N);
+  std::vector<int, NoInit<int>> host((size_t)4 * N);  // every node's four entries are written below
   int *nfirst = host.data(), *nt = nfirst + N, *ncb = nfirst + 2 * N, *nsc = nfirst + 3 * N;
   std::vector<int64_t> icnt(nitems, 0);
   std::vector<int> imu(nitems, 1), imc(nitems, 1);

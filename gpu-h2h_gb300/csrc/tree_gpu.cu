@@ -374,6 +374,10 @@ __global__ void level_key_kernel(const int *pre, const int *dep, int n, int heig
   }
 }
 
+__global__ void fill_value_kernel(int *a, int n, int value) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) a[i] = value;
+}
+
 __global__ void max_kernel(const int *a, int n, int *out) {
   int m = 0;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) m = max(m, a[i]);
@@ -456,10 +460,8 @@ void build_tree_gpu(Graph &g) {
   child_offsets_kernel<<<grid, 256, 0, s>>>(child_off, childs, size, n, g.head, A.fst, A.hp, A.sg, A.tl);
   GH_CUDA(cudaGetLastError());
   GH_CUDA(cudaMemcpy(A.anc, father, sizeof(int) * n, cudaMemcpyDeviceToDevice));
-  {
-    std::vector<int> ones(n, 1);
-    GH_CUDA(cudaMemcpy(A.dep, ones.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
-  }
+  fill_value_kernel<<<grid, 256, 0, s>>>(A.dep, n, 1);  // every depth starts at one step
+  GH_CUDA(cudaGetLastError());
   int rounds = 0;
   for (;;) {
     GH_CUDA(cudaMemsetAsync(more, 0, sizeof(int), s));
